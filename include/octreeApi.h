@@ -1,0 +1,120 @@
+/*
+ * OctreeApi -- C ABI of the GB300 LOD octree builder (libOctreeApi.so).
+ *
+ * Drop-in for the OctreeApi session API of PotreeConverterGPU.  The first 18
+ * entry points keep the reference's names, argument meaning, call order and
+ * return convention (0 = SUCCESS, -1 = UNEXPECTED_ERROR); each comment cites
+ * the reference declaration it replaces (OctreeApi/include/octreeApi.h) and
+ * implementation (OctreeApi/src/octreeApi.cpp, OctreeApi/src/session.cpp).
+ *
+ * Differences a caller can observe:
+ *   - CUDA and configuration errors return -1 (the reference calls exit(),
+ *     OctreeLibrary/include/defines.cuh:18-30); ocpi_last_error() describes
+ *     the last failure of the calling thread.
+ *   - Each session has its own device state, stream and statistics; sessions
+ *     on different host threads may run concurrently.
+ *   - octree.bin holds exactly the records referenced by hierarchy.bin (the
+ *     reference writes its whole, partly uninitialised, output buffer).
+ * Entry points after the first 18 are additions with no reference
+ * counterpart.
+ */
+#ifndef OCTREE_API_H
+#define OCTREE_API_H
+
+#include <stdbool.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+#define OCPI_EXPORT extern "C" __attribute__((visibility("default")))
+#else
+#define OCPI_EXPORT __attribute__((visibility("default")))
+#endif
+
+#define SUCCESS (0)
+#define UNEXPECTED_ERROR (-1)
+
+/* ---- session: octreeApi.h:42-44, octreeApi.cpp:96-128, session.cpp:87-112 */
+OCPI_EXPORT int ocpi_create_session(void** session, int device);
+OCPI_EXPORT int ocpi_destroy_session(void* session);
+/* 0 debug, 1 info, 2 warn, 3 error (octreeApi.cpp:96-115) */
+OCPI_EXPORT int ocpi_set_logging_level(int level);
+
+/* ---- cloud description: octreeApi.h:46-54, session.cpp:115-120,180-208 */
+/* 0 = float32 xyz + u8 rgb (15-byte records), 1 = float64 xyz + u8 rgb (27) */
+OCPI_EXPORT int ocpi_set_cloud_type(void* session, uint8_t cloudType);
+OCPI_EXPORT int ocpi_set_cloud_point_amount(void* session, uint32_t pointAmount);
+OCPI_EXPORT int ocpi_set_cloud_data_stride(void* session, uint32_t dataStride);
+OCPI_EXPORT int ocpi_set_cloud_scale(void* session, double x, double y, double z);
+/* stored only; no stage uses the offset (as in the reference) */
+OCPI_EXPORT int ocpi_set_cloud_offset(void* session, double x, double y, double z);
+/* the cubic bounding box (src/boundingbox.h:35-52 computes it in the CLI) */
+OCPI_EXPORT int ocpi_set_cloud_bb(void* session, double minX, double minY, double minZ, double maxX, double maxY,
+                                  double maxZ);
+/* borrowed host pointer, read by ocpi_init_octree */
+OCPI_EXPORT int ocpi_set_point_cloud_host(void* session, uint8_t* pointCloud);
+
+/* ---- configuration: octreeApi.h:56-65, session.cpp:158-179 */
+OCPI_EXPORT int ocpi_configure_chunking(void* session, uint32_t chunkingGrid, uint32_t mergingThreshold,
+                                        float outputFactor);
+OCPI_EXPORT int ocpi_configure_subsampling(void* session, uint32_t subsamplingGrid, bool intraCellAveraging,
+                                           bool interCellAveraging, bool replacementScheme,
+                                           bool useRandomSubsampling, bool useWeightingFunction);
+
+/* ---- reports: octreeApi.h:67-69, session.cpp:139-156 */
+OCPI_EXPORT int ocpi_export_memory_report(void* session, const char* filename);
+OCPI_EXPORT int ocpi_export_distribution_histogram(void* session, const char* filename, uint32_t binWidth);
+OCPI_EXPORT int ocpi_export_json_report(void* session, const char* filename);
+
+/* ---- pipeline: octreeApi.h:70-72, session.cpp:62-77,211-214 */
+OCPI_EXPORT int ocpi_export_potree(void* session, const char* directory);
+/* allocates device memory and uploads the cloud */
+OCPI_EXPORT int ocpi_init_octree(void* session);
+/* counting, merging, distribution and subsampling */
+OCPI_EXPORT int ocpi_generate_octree(void* session);
+
+/* ======================================================================= */
+/* Additions (no reference counterpart).                                   */
+
+/* Message of the last failed call on this host thread ("" if none). */
+OCPI_EXPORT const char* ocpi_last_error(void);
+/* Seed of the explicit-random subsampling priorities (default 0x5EED). */
+OCPI_EXPORT int ocpi_set_random_seed(void* session, uint64_t seed);
+/* Debug switches: bit 0 keeps a copy of the count pyramid (dense per level,
+ * z-major order) for ocpi_get_level_counts. */
+OCPI_EXPORT int ocpi_set_debug_flags(void* session, uint32_t flags);
+
+typedef struct OcpiStats {
+    uint64_t points_total;   /* records referenced by the hierarchy (N + subsampled) */
+    uint64_t p_out;          /* points held by internal nodes */
+    uint64_t p_in;           /* candidate points read by subsampling */
+    uint64_t out_capacity;   /* the reference's output buffer size for this config */
+    uint32_t depth;
+    uint32_t tree_nodes;
+    uint32_t leaf_nodes;
+    uint32_t internal_nodes;
+    uint32_t sparse_nodes;   /* occupied cells over all pyramid levels */
+    uint32_t dense_nodes;
+    uint32_t max_leaf_depth;
+    uint32_t min_leaf_points;
+    uint32_t max_leaf_points;
+    float mean_leaf_points;
+    float stdev_leaf_points;
+    uint32_t reserved;
+} OcpiStats;
+
+OCPI_EXPORT int ocpi_get_stats(void* session, OcpiStats* out);
+/* hierarchy.bin content: node_count entries of 22 bytes, BFS order */
+OCPI_EXPORT int ocpi_get_node_count(void* session, uint64_t* count);
+OCPI_EXPORT int ocpi_get_hierarchy(void* session, uint8_t* out);
+/* octree.bin content: points_total records of 18 bytes, and for each record
+ * the index of its source point in the cloud */
+OCPI_EXPORT int ocpi_get_records(void* session, uint8_t* out);
+OCPI_EXPORT int ocpi_get_lut(void* session, uint32_t* out);
+/* dense count grid of one pyramid level (requires debug bit 0) */
+OCPI_EXPORT int ocpi_get_level_counts(void* session, uint32_t level, uint32_t* out);
+/* Stage timings of the last ocpi_init_octree / ocpi_generate_octree, in ms,
+ * measured with CUDA events on the session stream.  Writes up to `max`
+ * values and their names (comma separated) into names (size name_bytes). */
+OCPI_EXPORT int ocpi_get_timings(void* session, double* ms, int max, char* names, int name_bytes, int* count);
+
+#endif /* OCTREE_API_H */

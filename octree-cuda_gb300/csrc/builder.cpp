@@ -1,0 +1,524 @@
+// Host orchestration of the LOD build.  Stage order and semantics follow
+// Session::generateOctree (OctreeApi/src/session.cpp:62-70): counting
+// (octree_chunking.cu:18-32), merging (:34-95), distribution (:97-124),
+// subsampling (octree_processor_impl.cu:164-186).  Tree bookkeeping that the
+// reference does on the host in double precision (node bounding boxes,
+// fp_subsampling.cu:15-61, tools.cu:29-61) is done here the same way.
+#include "builder.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+
+namespace oc {
+
+void check_cuda(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) throw Error(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+void BuildConfig::validate() const {
+    if (n == 0) throw Error("point amount is 0");
+    if (n >= 0x80000000u) throw Error("point amount must be below 2^31");
+    if (cloud_type > 1) throw Error("cloud type must be 0 (float) or 1 (double)");
+    uint32_t need = cloud_type == 0 ? 15u : 27u;
+    if (stride < need) throw Error("data stride too small for the cloud type");
+    if (chunk_grid < 2 || chunk_grid > 512 || (chunk_grid & (chunk_grid - 1)))
+        throw Error("chunking grid must be a power of two in [2, 512]");
+    if (sub_grid < 1 || sub_grid > 1024) throw Error("subsampling grid must be in [1, 1024]");
+    if (intra && weighting) throw Error("the weighting function requires inter-cell averaging without intra-cell");
+    if (!(bb_max[0] - bb_min[0] > 0.0)) throw Error("empty bounding box");
+    for (int a = 0; a < 3; ++a)
+        if (!(scale[a] > 0.0)) throw Error("scale must be positive");
+    if ((uint64_t)n * stride > (1ull << 40)) throw Error("cloud too large");
+}
+
+DevBuf::~DevBuf() {
+    release();
+}
+
+void DevBuf::release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+}
+
+void DevBuf::ensure(size_t b) {
+    if (b <= bytes && p) return;
+    release();
+    size_t want = std::max<size_t>(b, 256);
+    check_cuda(cudaMalloc(&p, want), "cudaMalloc");
+    bytes = want;
+}
+
+void DevBuf::ensure_keep(size_t b, size_t keep, cudaStream_t s) {
+    if (b <= bytes && p) return;
+    size_t want = std::max<size_t>(b + b / 4, 256);
+    void* np = nullptr;
+    check_cuda(cudaMalloc(&np, want), "cudaMalloc");
+    if (p && keep) check_cuda(cudaMemcpyAsync(np, p, std::min(keep, bytes), cudaMemcpyDeviceToDevice, s), "grow copy");
+    check_cuda(cudaStreamSynchronize(s), "grow sync");
+    release();
+    p = np;
+    bytes = want;
+}
+
+namespace {
+
+uint32_t ilog2(uint32_t g) {
+    uint32_t d = 0;
+    while ((1u << d) < g) ++d;
+    return d;
+}
+
+template <class T>
+void upload_vec(DevBuf& b, const std::vector<T>& v, cudaStream_t s) {
+    b.ensure(std::max<size_t>(v.size() * sizeof(T), 1));
+    if (!v.empty()) check_cuda(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s), "H2D");
+}
+
+}   // namespace
+
+Builder::Builder(const BuildConfig& cfg, const uint8_t* host_cloud, int device) : cfg_(cfg), device_(device) {
+    cfg_.validate();
+    check_cuda(cudaSetDevice(device_), "cudaSetDevice");
+    check_cuda(cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, device_), "device attribute");
+    check_cuda(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "stream");
+    depth_ = ilog2(cfg_.chunk_grid);
+    level_off_.assign(depth_ + 2, 0);
+    for (uint32_t l = 0; l <= depth_; ++l) {
+        uint64_t g = cfg_.chunk_grid >> l;
+        level_off_[l + 1] = level_off_[l] + g * g * g;
+    }
+    uint64_t cap = 1;
+    uint64_t per = cfg_.n / std::max<uint32_t>(cfg_.threshold, 1);
+    for (uint32_t l = 1; l <= depth_; ++l) {
+        uint64_t g = cfg_.chunk_grid >> l;
+        cap += 8 * std::min<uint64_t>(g * g * g, per);
+    }
+    node_cap_ = (uint32_t)std::min<uint64_t>(cap, level_off_[depth_ + 1]);
+
+    pyr_.ensure(level_off_[depth_ + 1] * 4);
+    loff_.ensure(level_off_.size() * 8);
+    check_cuda(cudaMemcpy(loff_.p, level_off_.data(), level_off_.size() * 8, cudaMemcpyHostToDevice), "H2D loff");
+    err_.ensure(64);
+    nonzero_.ensure((depth_ + 1) * 4);
+    key_.ensure((size_t)node_cap_ * 4);
+    count_.ensure((size_t)node_cap_ * 4);
+    level_.ensure((size_t)node_cap_);
+    info_.ensure((size_t)node_cap_ * 2);
+    child_first_.ensure((size_t)node_cap_ * 4);
+    level_start_.ensure((depth_ + 2) * 4);
+    n_nodes_.ensure(4);
+    cloud_.ensure((size_t)cfg_.n * cfg_.stride + 64);
+    lut_.ensure((size_t)cfg_.n * 4);
+    rec_.ensure((size_t)cfg_.n * 18);
+    upload(host_cloud);
+}
+
+Builder::~Builder() {
+    for (auto e : event_pool_) cudaEventDestroy(e);
+    if (stream_) cudaStreamDestroy(stream_);
+}
+
+void Builder::stage_begin() {
+    events_.clear();
+    stage_mark("begin");
+}
+
+void Builder::stage_mark(const char* name) {
+    size_t i = events_.size();
+    while (event_pool_.size() <= i) {
+        cudaEvent_t e;
+        check_cuda(cudaEventCreate(&e), "event");
+        event_pool_.push_back(e);
+    }
+    check_cuda(cudaEventRecord(event_pool_[i], stream_), "event record");
+    events_.push_back({name, event_pool_[i]});
+}
+
+void Builder::collect_timings() {
+    timings_.clear();
+    for (size_t i = 1; i < events_.size(); ++i) {
+        float ms = 0;
+        check_cuda(cudaEventElapsedTime(&ms, events_[i - 1].second, events_[i].second), "event time");
+        timings_.push_back({events_[i].first, ms});
+    }
+}
+
+void Builder::upload(const uint8_t* host_cloud) {
+    if (!host_cloud) throw Error("no point cloud set");
+    stage_begin();
+    check_cuda(cudaMemcpyAsync(cloud_.p, host_cloud, (size_t)cfg_.n * cfg_.stride, cudaMemcpyHostToDevice, stream_),
+               "cloud upload");
+    stage_mark("upload");
+    check_cuda(cudaStreamSynchronize(stream_), "upload sync");
+    collect_timings();
+}
+
+void Builder::check_device_errors(const char* stage) {
+    uint32_t e = 0;
+    check_cuda(cudaMemcpyAsync(&e, err_.p, 4, cudaMemcpyDeviceToHost, stream_), "D2H err");
+    check_cuda(cudaStreamSynchronize(stream_), stage);
+    if (e & kErrBelowBox) throw Error(std::string(stage) + ": a point lies below the bounding box");
+    if (e & kErrCoordRange) throw Error(std::string(stage) + ": an output coordinate does not fit int32");
+    if (e & kErrProbe) throw Error(std::string(stage) + ": subsampling brick table overflow");
+    if (e & kErrCapacity) throw Error(std::string(stage) + ": node capacity exceeded");
+    if (e & kErrTag) throw Error(std::string(stage) + ": a point found no leaf");
+}
+
+void Builder::generate() {
+    const double cubic = cfg_.bb_max[0] - cfg_.bb_min[0];
+    CloudGrid g;
+    g.grid = cfg_.chunk_grid;
+    const double t0 = cubic / cfg_.chunk_grid;   // kernel_helpers.cuh:14
+    for (int a = 0; a < 3; ++a) g.ax[a] = make_axis(cfg_.bb_min[a], t0);
+    OutParams op;
+    for (int a = 0; a < 3; ++a) op.ax[a] = make_out_axis(cfg_.bb_min[a], 1.0 / cfg_.scale[a]);   // octree_chunking.cu:109-111
+    const bool f32 = cfg_.cloud_type == 0;
+
+    stage_begin();
+    check_cuda(cudaMemsetAsync(pyr_.p, 0, level_off_[depth_ + 1] * 4, stream_), "memset");
+    check_cuda(cudaMemsetAsync(err_.p, 0, 64, stream_), "memset");
+    check_cuda(cudaMemsetAsync(nonzero_.p, 0, (depth_ + 1) * 4, stream_), "memset");
+    stage_mark("clear");
+    launch_count(cloud_.as<uint8_t>(), cfg_.n, cfg_.stride, f32, g, pyr_.as<uint32_t>(), err_.as<uint32_t>(),
+                 num_sms_, stream_);
+    stage_mark("count");
+    launch_pyramid(pyr_.as<uint32_t>(), level_off_.data(), depth_, nonzero_.as<uint32_t>(), stream_);
+    stage_mark("pyramid");
+    launch_enumerate(pyr_.as<uint32_t>(), loff_.as<uint64_t>(), depth_, cfg_.threshold, key_.as<uint32_t>(),
+                     count_.as<uint32_t>(), level_.as<uint8_t>(), info_.as<uint16_t>(), child_first_.as<uint32_t>(),
+                     node_cap_, level_start_.as<uint32_t>(), n_nodes_.as<uint32_t>(), err_.as<uint32_t>(), stream_);
+    stage_mark("tree");
+    check_cuda(cudaGetLastError(), "launch");
+    check_device_errors("counting");
+
+    uint32_t n_nodes = 0;
+    check_cuda(cudaMemcpy(&n_nodes, n_nodes_.p, 4, cudaMemcpyDeviceToHost), "D2H");
+    if (cfg_.debug & 1) {
+        pyramid_copy_.assign(depth_ + 1, {});
+        std::vector<uint32_t> tmp;
+        for (uint32_t l = 0; l <= depth_; ++l) {
+            uint64_t sz = level_off_[l + 1] - level_off_[l];
+            uint32_t gl = cfg_.chunk_grid >> l;
+            tmp.resize(sz);
+            check_cuda(cudaMemcpy(tmp.data(), pyr_.as<uint32_t>() + level_off_[l], sz * 4, cudaMemcpyDeviceToHost),
+                       "D2H pyramid");
+            auto& dst = pyramid_copy_[l];
+            dst.resize(sz);
+            for (uint32_t z = 0; z < gl; ++z)
+                for (uint32_t y = 0; y < gl; ++y)
+                    for (uint32_t x = 0; x < gl; ++x)
+                        dst[x + (uint64_t)y * gl + (uint64_t)z * gl * gl] = tmp[morton3(x, y, z)];
+        }
+    }
+    build_tree_host(n_nodes);
+
+    // leaf tags, then distribution
+    stage_mark("host_tree");
+    std::vector<uint64_t> didx(nodes_.size(), 0);
+    for (size_t i = 0; i < nodes_.size(); ++i) didx[i] = nodes_[i].data_idx;
+    upload_vec(leaves_, leaf_ids_, stream_);
+    upload_vec(data_idx_, didx, stream_);
+    fill_.ensure(nodes_.size() * 4);
+    check_cuda(cudaMemsetAsync(fill_.p, 0, nodes_.size() * 4, stream_), "memset");
+    launch_tag_leaves(pyr_.as<uint32_t>(), loff_.as<uint64_t>(), leaves_.as<uint32_t>(), (uint32_t)leaf_ids_.size(),
+                      key_.as<uint32_t>(), level_.as<uint8_t>(), stream_);
+    launch_distribute(cloud_.as<uint8_t>(), cfg_.n, cfg_.stride, f32, g, op, pyr_.as<uint32_t>(),
+                      loff_.as<uint64_t>(), depth_, data_idx_.as<uint64_t>(), fill_.as<uint32_t>(),
+                      lut_.as<uint32_t>(), rec_.as<uint8_t>(), err_.as<uint32_t>(), num_sms_, stream_);
+    stage_mark("distribute");
+    check_cuda(cudaGetLastError(), "launch");
+
+    subsample();
+    stage_mark("subsample");
+    place_internal();
+    stage_mark("place");
+    check_cuda(cudaGetLastError(), "launch");
+    check_device_errors("generate");
+    collect_timings();
+    compute_stats();
+}
+
+void Builder::build_tree_host(uint32_t n) {
+    std::vector<uint32_t> key(n), count(n), child_first(n);
+    std::vector<uint8_t> level(n);
+    std::vector<uint16_t> info(n);
+    check_cuda(cudaMemcpy(key.data(), key_.p, n * 4, cudaMemcpyDeviceToHost), "D2H");
+    check_cuda(cudaMemcpy(count.data(), count_.p, n * 4, cudaMemcpyDeviceToHost), "D2H");
+    check_cuda(cudaMemcpy(child_first.data(), child_first_.p, n * 4, cudaMemcpyDeviceToHost), "D2H");
+    check_cuda(cudaMemcpy(level.data(), level_.p, n, cudaMemcpyDeviceToHost), "D2H");
+    check_cuda(cudaMemcpy(info.data(), info_.p, n * 2, cudaMemcpyDeviceToHost), "D2H");
+    nodes_.assign(n, NodeHost{});
+    leaf_ids_.clear();
+    internal_by_level_.assign(depth_ + 1, {});
+    const double cubic = cfg_.bb_max[0] - cfg_.bb_min[0];
+    uint64_t off = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        NodeHost& v = nodes_[i];
+        v.key = key[i];
+        v.count = count[i];
+        v.level = level[i];
+        v.internal = info[i] & 1;
+        v.mask = (uint8_t)(info[i] >> 1);
+        v.child_first = child_first[i];
+        if (i == 0)
+            for (int a = 0; a < 3; ++a) v.mn[a] = cfg_.bb_min[a];
+        if (v.internal) {
+            internal_by_level_[v.level].push_back(i);
+            // children's bbox minimum: parent min + childBBSide per set slot bit
+            double side = cubic / std::pow(2.0, (double)(depth_ - v.level));
+            double cside = side / 2.0;
+            uint32_t c = v.child_first;
+            for (uint32_t s = 0; s < 8; ++s) {
+                if (!(v.mask & (1u << s))) continue;
+                NodeHost& ch = nodes_[c];
+                ch.mn[0] = (s & 4) ? v.mn[0] + cside : v.mn[0];
+                ch.mn[1] = (s & 2) ? v.mn[1] + cside : v.mn[1];
+                ch.mn[2] = (s & 1) ? v.mn[2] + cside : v.mn[2];
+                ++c;
+            }
+        } else {
+            v.points = v.count;
+            v.data_idx = off;
+            off += v.count;
+            leaf_ids_.push_back(i);
+        }
+    }
+    if (off != cfg_.n) throw Error("leaf points do not add up to the point amount");
+}
+
+void Builder::subsample() {
+    const double cubic = cfg_.bb_max[0] - cfg_.bb_min[0];
+    const uint32_t S = cfg_.sub_grid;
+    uint32_t mode = 0;
+    if (cfg_.intra) mode |= kModeIntra;
+    if (cfg_.inter) mode |= kModeInter;
+    if (cfg_.random) mode |= kModeRandom;
+    if (cfg_.weighting) mode |= kModeWeight;
+    const bool intra = cfg_.intra;
+    const bool inter = !intra && cfg_.inter;
+    const bool weighted = inter && cfg_.weighting;
+    const bool averaged = intra || inter;
+    stage_used_ = 0;
+    stats_.p_in = 0;
+    OutParams op;
+    for (int a = 0; a < 3; ++a) op.ax[a] = make_out_axis(cfg_.bb_min[a], 1.0 / cfg_.scale[a]);
+
+    for (uint32_t l = 1; l <= depth_; ++l) {
+        const auto& list = internal_by_level_[l];
+        if (list.empty()) continue;
+        const double side = cubic / std::pow(2.0, (double)(depth_ - l));   // fp_subsampling.cu:16-17
+        const double t = side / S;                                         // kernel_helpers.cuh:14
+        std::vector<SubNode> table(list.size());
+        uint64_t level_in = 0;
+        for (size_t k = 0; k < list.size(); ++k) {
+            const NodeHost& v = nodes_[list[k]];
+            SubNode& sn = table[k];
+            std::memset(&sn, 0, sizeof(sn));
+            for (int a = 0; a < 3; ++a) sn.ax[a] = make_axis(v.mn[a], t);
+            sn.morton = v.key;
+            sn.level = l;
+            uint32_t c = v.child_first, nc = 0;
+            uint64_t p = 0;
+            for (uint32_t s = 0; s < 8; ++s) {
+                if (!(v.mask & (1u << s))) continue;
+                const NodeHost& ch = nodes_[c++];
+                if (ch.internal) {
+                    sn.child_kind |= 1u << nc;
+                    sn.child_start[nc] = ch.stage_off;
+                } else {
+                    sn.child_start[nc] = ch.data_idx;
+                }
+                sn.child_count[nc] = ch.points;
+                p += ch.points;
+                ++nc;
+            }
+            sn.nchild = nc;
+            if (p > 0xFFFFFFFFull) throw Error("internal node too large");
+            sn.p_in = (uint32_t)p;
+            sn.cand_off = level_in;
+            level_in += p;
+        }
+        stats_.p_in += level_in;
+        // scratch and staging capacity
+        key_cache_.ensure(level_in * 4);
+        acc_best_.ensure(level_in * 8);
+        if (averaged && !weighted) acc_intra_.ensure(level_in * 8);
+        if (weighted) {
+            unit_cache_.ensure(level_in * 12);
+            csr_count_.ensure(level_in * 4);
+            csr_start_.ensure(level_in * 4);
+            csr_pts_.ensure(level_in * 20);
+        }
+        uint64_t need = stage_used_ + level_in;
+        stage_lut_.ensure_keep(need * 4, stage_used_ * 4, stream_);
+        stage_rec_.ensure_keep(need * 18, stage_used_ * 18, stream_);
+        upload_vec(sub_nodes_, table, stream_);
+        out_points_.ensure(list.size() * 4);
+        work_.ensure(4);
+        check_cuda(cudaMemsetAsync(work_.p, 0, 4, stream_), "memset");
+
+        SubLevelArgs a{};
+        a.nodes = sub_nodes_.as<SubNode>();
+        a.n_nodes = (uint32_t)list.size();
+        a.grid = S;
+        a.mode = mode;
+        a.float_input = cfg_.cloud_type == 0;
+        a.seed = cfg_.seed;
+        a.cloud = cloud_.as<uint8_t>();
+        a.stride = cfg_.stride;
+        a.leaf_lut = lut_.as<uint32_t>();
+        a.leaf_rec = rec_.as<uint8_t>();
+        a.stage_lut = stage_lut_.as<uint32_t>();
+        a.stage_rec = stage_rec_.as<uint8_t>();
+        a.out_lut = stage_lut_.as<uint32_t>() + stage_used_;
+        a.out_rec = stage_rec_.as<uint8_t>() + stage_used_ * 18;
+        a.out_points = out_points_.as<uint32_t>();
+        a.key_cache = key_cache_.as<uint32_t>();
+        a.unit_cache = unit_cache_.as<float>();
+        a.acc_best = acc_best_.as<uint64_t>();
+        a.acc_intra = acc_intra_.as<uint64_t>();
+        a.csr_count = csr_count_.as<uint32_t>();
+        a.csr_start = csr_start_.as<uint32_t>();
+        a.csr_pts = csr_pts_.as<uint8_t>();
+        a.out = op;
+        a.work_counter = work_.as<uint32_t>();
+        a.err = err_.as<uint32_t>();
+        launch_subsample_level(a, num_sms_, stream_);
+        check_cuda(cudaGetLastError(), "subsample launch");
+        std::vector<uint32_t> pts(list.size());
+        check_cuda(cudaMemcpyAsync(pts.data(), out_points_.p, pts.size() * 4, cudaMemcpyDeviceToHost, stream_), "D2H");
+        check_cuda(cudaStreamSynchronize(stream_), "subsample level");
+        for (size_t k = 0; k < list.size(); ++k) {
+            NodeHost& v = nodes_[list[k]];
+            v.points = pts[k];
+            v.stage_off = stage_used_ + table[k].cand_off;
+        }
+        stage_used_ += level_in;
+    }
+}
+
+void Builder::place_internal() {
+    // DFS post-order after the N leaf points (calculateWritingPosition,
+    // kernel_helpers.cuh:55-59; setActiveParent fp_subsampling.cu:183)
+    std::vector<uint64_t> src, dst;
+    std::vector<uint32_t> cnt;
+    uint64_t off = cfg_.n;
+    std::vector<std::pair<uint32_t, bool>> st{{0u, false}};
+    while (!st.empty()) {
+        auto [i, expanded] = st.back();
+        st.pop_back();
+        NodeHost& v = nodes_[i];
+        if (!v.internal) continue;
+        if (expanded) {
+            v.data_idx = off;
+            off += v.points;
+            src.push_back(v.stage_off);
+            dst.push_back(v.data_idx);
+            cnt.push_back(v.points);
+            continue;
+        }
+        st.push_back({i, true});
+        std::vector<uint32_t> kids;
+        uint32_t c = v.child_first;
+        for (uint32_t s = 0; s < 8; ++s)
+            if (v.mask & (1u << s)) kids.push_back(c++);
+        for (auto it = kids.rbegin(); it != kids.rend(); ++it) st.push_back({*it, false});
+    }
+    p_out_ = off - cfg_.n;
+    uint64_t total = off;
+    lut_.ensure_keep(total * 4, (size_t)cfg_.n * 4, stream_);
+    rec_.ensure_keep(total * 18, (size_t)cfg_.n * 18, stream_);
+    upload_vec(place_src_, src, stream_);
+    upload_vec(place_dst_, dst, stream_);
+    upload_vec(place_cnt_, cnt, stream_);
+    launch_place(place_src_.as<uint64_t>(), place_dst_.as<uint64_t>(), place_cnt_.as<uint32_t>(), (uint32_t)cnt.size(),
+                 stage_lut_.as<uint32_t>(), stage_rec_.as<uint8_t>(), lut_.as<uint32_t>(), rec_.as<uint8_t>(),
+                 stream_);
+}
+
+void Builder::compute_stats() {
+    Stats& S = stats_;
+    S.depth = depth_;
+    S.tree_nodes = (uint32_t)nodes_.size();
+    S.leaf_nodes = (uint32_t)leaf_ids_.size();
+    S.internal_nodes = S.tree_nodes - S.leaf_nodes;
+    S.p_out = p_out_;
+    S.points_total = (uint64_t)cfg_.n + p_out_;
+    S.out_capacity = (uint64_t)((float)cfg_.n * cfg_.output_factor);   // point_cloud.cuh:24
+    S.dense_nodes = (uint32_t)level_off_[depth_ + 1];
+    std::vector<uint32_t> nz(depth_ + 1);
+    check_cuda(cudaMemcpy(nz.data(), nonzero_.p, nz.size() * 4, cudaMemcpyDeviceToHost), "D2H");
+    S.sparse_nodes = 0;
+    for (uint32_t v : nz) S.sparse_nodes += v;
+    // OctreeData::updateNodeStatistics (octree.cu:79-132): DFS in slot order
+    S.min_leaf_points = 0xFFFFFFFFu;
+    S.max_leaf_points = 0;
+    S.max_leaf_depth = 0;
+    uint32_t sum = 0;
+    std::vector<uint32_t> order;
+    std::vector<std::pair<uint32_t, uint32_t>> st{{0u, 0u}};
+    while (!st.empty()) {
+        auto [i, d] = st.back();
+        st.pop_back();
+        const NodeHost& v = nodes_[i];
+        if (!v.internal) {
+            S.max_leaf_depth = std::max(S.max_leaf_depth, d);
+            sum += v.count;
+            S.min_leaf_points = std::min(S.min_leaf_points, v.count);
+            S.max_leaf_points = std::max(S.max_leaf_points, v.count);
+            order.push_back(i);
+            continue;
+        }
+        std::vector<uint32_t> kids;
+        uint32_t c = v.child_first;
+        for (uint32_t s = 0; s < 8; ++s)
+            if (v.mask & (1u << s)) kids.push_back(c++);
+        for (auto it = kids.rbegin(); it != kids.rend(); ++it) st.push_back({*it, d + 1});
+    }
+    S.mean_leaf_points = (float)sum / (float)S.leaf_nodes;
+    float var = 0.f;
+    for (uint32_t i : order) {
+        float d = (float)nodes_[i].count - S.mean_leaf_points;
+        var += std::pow(d, 2.f);
+    }
+    S.stdev_leaf_points = std::sqrt(var / (float)S.leaf_nodes);
+}
+
+std::vector<uint8_t> Builder::hierarchy() const {
+    std::vector<uint8_t> out(nodes_.size() * 22);
+    for (size_t i = 0; i < nodes_.size(); ++i) {
+        const NodeHost& v = nodes_[i];
+        uint8_t mask = v.internal ? v.mask : 0;
+        uint8_t type = mask == 0 ? 1 : 0;
+        uint32_t pts = v.points;
+        uint64_t off = v.data_idx * 18ull, size = (uint64_t)pts * 18ull;
+        uint8_t* e = out.data() + i * 22;
+        e[0] = type;
+        e[1] = mask;
+        std::memcpy(e + 2, &pts, 4);
+        std::memcpy(e + 6, &off, 8);
+        std::memcpy(e + 14, &size, 8);
+    }
+    return out;
+}
+
+void Builder::copy_records(uint8_t* out) const {
+    check_cuda(cudaMemcpy(out, rec_.p, stats_.points_total * 18, cudaMemcpyDeviceToHost), "D2H records");
+}
+
+void Builder::copy_lut(uint32_t* out) const {
+    check_cuda(cudaMemcpy(out, lut_.p, stats_.points_total * 4, cudaMemcpyDeviceToHost), "D2H lut");
+}
+
+bool Builder::level_counts(uint32_t level, uint32_t* out) const {
+    if (level >= pyramid_copy_.size()) return false;
+    std::memcpy(out, pyramid_copy_[level].data(), pyramid_copy_[level].size() * 4);
+    return true;
+}
+
+}   // namespace oc

@@ -1,0 +1,145 @@
+// LOD octree builder: owns the device state of one session and runs the
+// stages of the OctreeApi pipeline (OctreeProcessorImpl in the reference,
+// OctreeLibrary/src/include/octree_processor_impl.cuh:14-71).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "kernels.h"
+
+namespace oc {
+
+struct Error : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+
+void check_cuda(cudaError_t e, const char* what);
+
+// PointCloudInfo + ProcessingInfo (OctreeLibrary/include/metadata.cuh:55-101).
+struct BuildConfig {
+    uint32_t n = 0;
+    uint32_t stride = 0;
+    uint32_t cloud_type = 0;
+    double scale[3] = {1, 1, 1};
+    double offset[3] = {0, 0, 0};
+    double bb_min[3] = {0, 0, 0};
+    double bb_max[3] = {0, 0, 0};
+    uint32_t chunk_grid = 0;
+    uint32_t threshold = 0;
+    float output_factor = 0.f;
+    uint32_t sub_grid = 0;
+    bool intra = false, inter = false, replacement = false, random = false, weighting = false;
+    uint64_t seed = 0x5EED;
+    uint32_t debug = 0;
+
+    void validate() const;
+};
+
+// Grow-only device allocation.
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf();
+    void ensure(size_t b);
+    void ensure_keep(size_t b, size_t keep, cudaStream_t s);   // grow, preserving the first `keep` bytes
+    void release();
+    template <class T>
+    T* as() const {
+        return static_cast<T*>(p);
+    }
+};
+
+struct NodeHost {
+    uint32_t key;          // Morton key within its level
+    uint32_t count;        // pyramid count (points below the cell)
+    uint32_t level;        // 0 = finest chunking level
+    uint32_t child_first;  // BFS index of the first child (internal nodes)
+    uint8_t internal;
+    uint8_t mask;          // occupied children (internal nodes)
+    uint32_t points;       // points referenced by the hierarchy entry
+    uint64_t data_idx;     // first record in octree.bin
+    uint64_t stage_off;    // staged position of an internal node's output
+    double mn[3];          // bbox minimum (calculateChildMinBB chain)
+};
+
+struct Stats {
+    uint64_t points_total = 0, p_out = 0, p_in = 0, out_capacity = 0;
+    uint32_t depth = 0, tree_nodes = 0, leaf_nodes = 0, internal_nodes = 0, sparse_nodes = 0, dense_nodes = 0;
+    uint32_t max_leaf_depth = 0, min_leaf_points = 0, max_leaf_points = 0;
+    float mean_leaf_points = 0.f, stdev_leaf_points = 0.f;
+};
+
+class Builder {
+public:
+    Builder(const BuildConfig& cfg, const uint8_t* host_cloud, int device);
+    ~Builder();
+    Builder(const Builder&) = delete;
+    Builder& operator=(const Builder&) = delete;
+
+    // Uploads a new cloud of the same configuration (reuses allocations).
+    void upload(const uint8_t* host_cloud);
+    void generate();
+    void export_potree(const std::string& dir) const;
+    void export_json_report(const std::string& file) const;
+    void export_histogram(const std::string& file, uint32_t bin_width) const;
+
+    const Stats& stats() const { return stats_; }
+    const std::vector<NodeHost>& nodes() const { return nodes_; }
+    std::vector<uint8_t> hierarchy() const;
+    void copy_records(uint8_t* out) const;
+    void copy_lut(uint32_t* out) const;
+    bool level_counts(uint32_t level, uint32_t* out) const;
+    const std::vector<std::pair<std::string, double>>& timings() const { return timings_; }
+    cudaStream_t stream() const { return stream_; }
+    const BuildConfig& config() const { return cfg_; }
+
+private:
+    void stage_mark(const char* name);
+    void stage_begin();
+    void collect_timings();
+    void check_device_errors(const char* stage);
+    void build_tree_host(uint32_t n_nodes);
+    void subsample();
+    void place_internal();
+    void compute_stats();
+
+    BuildConfig cfg_;
+    int device_ = 0;
+    int num_sms_ = 0;
+    cudaStream_t stream_ = nullptr;
+    uint32_t depth_ = 0;
+    std::vector<uint64_t> level_off_;   // pyramid level offsets (cells), depth + 2 entries
+    uint32_t node_cap_ = 0;
+
+    DevBuf cloud_, pyr_, loff_, err_, nonzero_;
+    DevBuf key_, count_, level_, info_, child_first_, level_start_, n_nodes_;
+    DevBuf leaves_, data_idx_, fill_;
+    DevBuf lut_, rec_;                  // final outputs (N + P_out records)
+    DevBuf stage_lut_, stage_rec_;      // staged internal outputs
+    DevBuf sub_nodes_, out_points_, work_;
+    DevBuf key_cache_, unit_cache_, acc_best_, acc_intra_, acc_w_, csr_count_, csr_start_, csr_pts_;
+    DevBuf place_src_, place_dst_, place_cnt_;
+
+    std::vector<NodeHost> nodes_;
+    std::vector<uint32_t> leaf_ids_;
+    std::vector<std::vector<uint32_t>> internal_by_level_;
+    std::vector<std::vector<uint32_t>> pyramid_copy_;
+    uint64_t p_out_ = 0;
+    uint64_t stage_used_ = 0;
+    Stats stats_;
+
+    std::vector<std::pair<std::string, cudaEvent_t>> events_;
+    std::vector<cudaEvent_t> event_pool_;
+    std::vector<std::pair<std::string, double>> timings_;
+};
+
+}   // namespace oc

@@ -1,0 +1,367 @@
+// Device-side arithmetic shared by every stage of the LOD build.
+//
+// Exactness contract.  The reference maps a coordinate to a grid cell with
+// IEEE binary64 arithmetic (mapPointToGrid, OctreeLibrary/src/kernel/
+// kernel_helpers.cuh:10-25) and quantises output coordinates the same way
+// (point_distributing.cuh:245-247).  GB300's binary64 issue rate is a small
+// fraction of its binary32 rate, so every stage evaluates those formulas with
+// an fp32 (or float-float) estimate plus a rigorous error bound, and only
+// falls back to the binary64 expression when the estimate lies within that
+// bound of a cell boundary.  The result is always the binary64 result.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace oc {
+
+constexpr uint32_t kNoCell = 0xFFFFFFFFu;
+
+// ---------------------------------------------------------------------------
+// Cell index along one axis of a gridding.
+
+struct AxisGrid {
+    double mn;    // bounding-box minimum of the gridded cube
+    double t;     // cell size = cube side / grid, as the reference computes it
+    float m_hi;   // float(mn)
+    float m_lo;   // float(mn - m_hi)
+    float r;      // float(1 / t)
+    float cm;     // 2^-44 * |mn| / t : absolute part of the error bound
+};
+
+__host__ __device__ inline AxisGrid make_axis(double mn, double t) {
+    AxisGrid a;
+    a.mn = mn;
+    a.t = t;
+    a.m_hi = (float)mn;
+    a.m_lo = (float)(mn - (double)a.m_hi);
+    a.r = (float)(1.0 / t);
+    double cm = 5.684341886080802e-14 * (mn < 0 ? -mn : mn) / t;   // 2^-44
+    a.cm = (float)(cm * 1.0000001) + 1e-30f;
+    return a;
+}
+
+// ---------------------------------------------------------------------------
+// Output coordinate floor((p - mn) * sf) as int32 (the reference's
+// static_cast<int32_t>(floor(...)), point_distributing.cuh:245-247).
+
+struct OutAxis {
+    double mn;
+    double sf;    // 1 / scale, computed in double on the host
+    float m_hi, m_lo;
+    float sf_hi, sf_lo;
+};
+
+__host__ __device__ inline OutAxis make_out_axis(double mn, double sf) {
+    OutAxis o;
+    o.mn = mn;
+    o.sf = sf;
+    o.m_hi = (float)mn;
+    o.m_lo = (float)(mn - (double)o.m_hi);
+    o.sf_hi = (float)sf;
+    o.sf_lo = (float)(sf - (double)o.sf_hi);
+    return o;
+}
+
+constexpr int32_t kCoordError = (int32_t)0x80000000;
+
+// ---------------------------------------------------------------------------
+// Morton order with x as the most significant bit of every triple: the child
+// slot of a cell inside its parent is the low three bits (x<<2 | y<<1 | z),
+// the same slot numbering as the reference (point_count_propagation.cuh:241-249).
+
+__host__ __device__ inline uint32_t spread3(uint32_t v) {
+    v &= 0x3FFu;
+    v = (v | (v << 16)) & 0x030000FFu;
+    v = (v | (v << 8)) & 0x0300F00Fu;
+    v = (v | (v << 4)) & 0x030C30C3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
+__host__ __device__ inline uint32_t morton3(uint32_t x, uint32_t y, uint32_t z) {
+    return (spread3(x) << 2) | (spread3(y) << 1) | spread3(z);
+}
+
+__host__ __device__ inline uint32_t compact3(uint32_t v) {
+    v &= 0x09249249u;
+    v = (v | (v >> 2)) & 0x030C30C3u;
+    v = (v | (v >> 4)) & 0x0300F00Fu;
+    v = (v | (v >> 8)) & 0x030000FFu;
+    v = (v | (v >> 16)) & 0x000003FFu;
+    return v;
+}
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11): priority of a cloud point
+// for explicit random subsampling in node (level, morton).
+
+__host__ __device__ inline uint32_t rp_priority(uint64_t seed, uint32_t level, uint64_t morton, uint32_t idx) {
+    uint32_t c0 = idx, c1 = (uint32_t)morton, c2 = (uint32_t)(morton >> 32) ^ (level << 24), c3 = 0x52504E44u;
+    uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+        uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+        uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0;
+        uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
+        c1 = (uint32_t)p1;
+        c3 = (uint32_t)p0;
+        c0 = n0;
+        c2 = n2;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    return c0;
+}
+
+// Device error bits (sticky, read by the host after each stage).
+enum : uint32_t {
+    kErrBelowBox = 1u << 0,      // a point maps below the bounding box
+    kErrCoordRange = 1u << 1,    // an output coordinate does not fit int32
+    kErrProbe = 1u << 2,         // a hash probe exceeded its bound
+    kErrCapacity = 1u << 3,      // a scratch buffer was too small
+    kErrTag = 1u << 4,           // a point found no leaf
+};
+
+#if defined(__CUDACC__)
+// ===== device-only arithmetic =====
+
+// ---------------------------------------------------------------------------
+// Coordinates: a point coordinate as an unevaluated float pair hi + lo.
+
+struct Coord {
+    float hi, lo;
+    bool ok;        // split valid (otherwise only the exact path is used)
+    double exact;   // the coordinate as binary64 (converted lazily for float input)
+};
+
+// float input: hi = value, lo = 0 (exact).
+__device__ __forceinline__ Coord coord_f32(float f) {
+    Coord c;
+    c.hi = f;
+    c.lo = 0.0f;
+    c.ok = true;
+    c.exact = 0.0;   // filled by exact_value() on demand
+    return c;
+}
+
+// double input: hi = value with its mantissa truncated to 24 bits, lo = the
+// remainder rounded to float.  Built from integer operations only.
+__device__ __forceinline__ Coord coord_f64(double d) {
+    Coord c;
+    c.exact = d;
+    unsigned long long bits = (unsigned long long)__double_as_longlong(d);
+    unsigned e = (unsigned)(bits >> 52) & 0x7FFu;
+    unsigned long long mant = bits & ((1ull << 52) - 1);
+    unsigned sign = (unsigned)(bits >> 63) << 31;
+    if (e == 0 && mant == 0) {
+        c.hi = __uint_as_float(sign);
+        c.lo = 0.0f;
+        c.ok = true;
+        return c;
+    }
+    int ue = (int)e - 1023;
+    if (ue < -60 || ue > 100) {
+        c.hi = c.lo = 0.0f;
+        c.ok = false;
+        return c;
+    }
+    c.hi = __uint_as_float(sign | ((unsigned)(ue + 127) << 23) | (unsigned)(mant >> 29));
+    unsigned low = (unsigned)(mant & ((1u << 29) - 1));
+    if (low == 0) {
+        c.lo = 0.0f;
+    } else {
+        float lf = __fmul_rn(__uint2float_rn(low), __uint_as_float((unsigned)(ue - 52 + 127) << 23));
+        c.lo = sign ? -lf : lf;
+    }
+    c.ok = true;
+    return c;
+}
+
+// Cell-unit position (p - mn) / t in fp32 from the split coordinate.
+__device__ __forceinline__ float approx_units(const Coord& c, const AxisGrid& a) {
+    float s = __fsub_rn(c.hi, a.m_hi);
+    float q = __fsub_rn(c.lo, a.m_lo);
+    float d = __fadd_rn(s, q);
+    return __fmul_rn(d, a.r);
+}
+
+__device__ __forceinline__ int idx_from_units(float x, uint32_t G) {
+    if (x >= (float)(G - 1)) return (int)G - 1;
+    if (!(x > -1.0f)) return -1;
+    return x < 0.0f ? 0 : (int)x;
+}
+
+// Binary64 evaluation of mapPointToGrid for one axis: (int64)fmin((p-mn)/t, G-1).
+// Returns -1 where the reference would produce a negative index.
+static __device__ __noinline__ int exact_axis_cell(double p, double mn, double t, uint32_t G) {
+    double u = __ddiv_rn(__dsub_rn(p, mn), t);
+    double v = fmin(u, (double)G - 1.0);
+    if (!(v > -1.0)) return -1;
+    return (int)(long long)v;
+}
+
+template <bool kFloatInput>
+__device__ __forceinline__ double exact_value(const Coord& c) {
+    return kFloatInput ? (double)c.hi : c.exact;
+}
+
+// Cell index of one axis; `units` receives the fp32 cell-unit position.
+template <bool kFloatInput>
+__device__ __forceinline__ int axis_cell(const Coord& c, const AxisGrid& a, uint32_t G, float& units) {
+    if (kFloatInput || c.ok) {
+        float A = approx_units(c, a);
+        units = A;
+        float eps = __fmaf_rn(fabsf(A), 9.5367431640625e-07f, __fadd_rn(9.5367431640625e-07f, a.cm));   // 2^-20
+        int lo = idx_from_units(__fsub_rn(A, eps), G);
+        int hi = idx_from_units(__fadd_rn(A, eps), G);
+        if (lo == hi && lo >= 0) return lo;
+    } else {
+        units = (float)((exact_value<kFloatInput>(c) - a.mn) / a.t);
+    }
+    return exact_axis_cell(exact_value<kFloatInput>(c), a.mn, a.t, G);
+}
+
+static __device__ __noinline__ int32_t exact_out_coord(double p, double mn, double sf) {
+    double v = floor(__dmul_rn(__dsub_rn(p, mn), sf));
+    if (!(v > -2147483648.0 && v < 2147483648.0)) return kCoordError;
+    return (int32_t)v;
+}
+
+template <bool kFloatInput>
+__device__ __forceinline__ int32_t out_coord(const Coord& c, const OutAxis& o) {
+    if (kFloatInput || c.ok) {
+        // s + e1 = hi - m_hi exactly (Knuth TwoSum)
+        float nm = -o.m_hi;
+        float s = __fadd_rn(c.hi, nm);
+        float bb = __fsub_rn(s, c.hi);
+        float e1 = __fadd_rn(__fsub_rn(c.hi, __fsub_rn(s, bb)), __fsub_rn(nm, bb));
+        float lo2 = __fsub_rn(__fadd_rn(e1, c.lo), o.m_lo);
+        float ph = __fmul_rn(s, o.sf_hi);
+        float perr = __fmaf_rn(s, o.sf_hi, -ph);
+        float pl = __fmaf_rn(s, o.sf_lo, __fmaf_rn(lo2, o.sf_hi, perr));
+        if (fabsf(ph) < 1.0e9f) {
+            float f = floorf(ph);
+            float frac = __fadd_rn(__fsub_rn(ph, f), pl);
+            float g = floorf(frac);
+            float rem = __fsub_rn(frac, g);
+            float mag = __fmaf_rn(__fadd_rn(fabsf(c.hi), fabsf(o.m_hi)), fabsf(o.sf_hi), fabsf(ph));
+            float E = __fmaf_rn(mag, 2.2737367544323206e-13f, 2.384185791015625e-07f);   // 2^-42, 2^-22
+            if (rem >= E && rem <= __fsub_rn(1.0f, E)) return (int32_t)f + (int32_t)g;
+        }
+    }
+    return exact_out_coord(exact_value<kFloatInput>(c), o.mn, o.sf);
+}
+
+// ---------------------------------------------------------------------------
+// Packed colour sums (encodeColors kernel_helpers.cuh:49-53, decode
+// fp_subsampling.cuh:95-101).  A zero count field (a multiple of 1024 points)
+// divides by zero in the reference; here it yields 0xFFFF.
+
+__device__ __forceinline__ uint64_t encode_colors(uint32_t r, uint32_t g, uint32_t b) {
+    return ((uint64_t)r << 46) | ((uint64_t)g << 28) | ((uint64_t)b << 10) | 1ull;
+}
+
+__device__ __forceinline__ void decode_colors(uint64_t e, uint16_t& r, uint16_t& g, uint16_t& b) {
+    uint32_t amount = (uint32_t)(e & 0x3FF);
+    if (amount == 0) {
+        r = g = b = 0xFFFF;
+        return;
+    }
+    r = (uint16_t)((uint32_t)((e >> 46) & 0xFFFF) / amount);
+    g = (uint16_t)((uint32_t)((e >> 28) & 0xFFFF) / amount);
+    b = (uint16_t)((uint32_t)((e >> 10) & 0xFFFF) / amount);
+}
+
+// ---------------------------------------------------------------------------
+// Distance weighting.  exp(x) for x in [-15, 0] by Cody & Waite range
+// reduction and the degree-7 Taylor polynomial of e^f (Horner, fused
+// multiply-adds), then exact scaling by 2^k.  The weight of a point at cell
+// units u for neighbour cell n is round(2^20 * exp(-10 * |n + 0.5 - u|^2 * 4/27)),
+// i.e. exp(-10 (d/r)^2) with r the half diagonal of 3x3x3 cells
+// (kernel_inter_cell_filtering.cuh:171-180, fp_subsampling.cu:56-61).
+
+__device__ __forceinline__ float exp_neg(float x) {
+    const float kLog2e = 1.44269504088896341f;
+    const float kLn2Hi = 0.693359375f;
+    const float kLn2Lo = -2.12194440054690583e-4f;
+    float kf = rintf(__fmul_rn(x, kLog2e));
+    float f = __fmaf_rn(-kf, kLn2Hi, x);
+    f = __fmaf_rn(-kf, kLn2Lo, f);
+    float p = 1.0f / 5040.0f;
+    p = __fmaf_rn(p, f, 1.0f / 720.0f);
+    p = __fmaf_rn(p, f, 1.0f / 120.0f);
+    p = __fmaf_rn(p, f, 1.0f / 24.0f);
+    p = __fmaf_rn(p, f, 1.0f / 6.0f);
+    p = __fmaf_rn(p, f, 0.5f);
+    p = __fmaf_rn(p, f, 1.0f);
+    p = __fmaf_rn(p, f, 1.0f);
+    int k = (int)kf;
+    return __fmul_rn(p, __uint_as_float((unsigned)(k + 127) << 23));
+}
+
+__device__ __forceinline__ uint32_t weight_q(float ux, float uy, float uz, int nx, int ny, int nz) {
+    float dx = __fsub_rn(__fadd_rn((float)nx, 0.5f), ux);
+    float dy = __fsub_rn(__fadd_rn((float)ny, 0.5f), uy);
+    float dz = __fsub_rn(__fadd_rn((float)nz, 0.5f), uz);
+    float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+    float q = __fmul_rn(d2, (float)(4.0 / 27.0));
+    q = fminf(q, 1.5f);
+    float w = exp_neg(__fmul_rn(-10.0f, q));
+    return (uint32_t)__fadd_rn(__fmul_rn(w, 1048576.0f), 0.5f);
+}
+
+// ---------------------------------------------------------------------------
+// Record I/O.
+
+struct __align__(2) Record18 {   // OutputBuffer, types.cuh:18-24 (packed, 18 bytes)
+    uint16_t h[9];
+};
+
+__device__ __forceinline__ void store_record(uint8_t* base, uint64_t pos, int32_t x, int32_t y, int32_t z, uint16_t r,
+                                             uint16_t g, uint16_t b) {
+    uint16_t* p = reinterpret_cast<uint16_t*>(base + pos * 18);
+    p[0] = (uint16_t)x;
+    p[1] = (uint16_t)((uint32_t)x >> 16);
+    p[2] = (uint16_t)y;
+    p[3] = (uint16_t)((uint32_t)y >> 16);
+    p[4] = (uint16_t)z;
+    p[5] = (uint16_t)((uint32_t)z >> 16);
+    p[6] = r;
+    p[7] = g;
+    p[8] = b;
+}
+
+// Unaligned little-endian loads of a cloud record (15- or 27-byte stride).
+__device__ __forceinline__ uint32_t load_u32_unaligned(const uint8_t* p) {
+    return (uint32_t)p[0] | ((uint32_t)p[1] << 8) | ((uint32_t)p[2] << 16) | ((uint32_t)p[3] << 24);
+}
+
+__device__ __forceinline__ uint64_t load_u64_unaligned(const uint8_t* p) {
+    return (uint64_t)load_u32_unaligned(p) | ((uint64_t)load_u32_unaligned(p + 4) << 32);
+}
+
+template <bool kFloatInput>
+__device__ __forceinline__ void load_point(const uint8_t* rec, Coord c[3], uint32_t col[3]) {
+    if (kFloatInput) {
+        c[0] = coord_f32(__uint_as_float(load_u32_unaligned(rec)));
+        c[1] = coord_f32(__uint_as_float(load_u32_unaligned(rec + 4)));
+        c[2] = coord_f32(__uint_as_float(load_u32_unaligned(rec + 8)));
+        col[0] = rec[12];
+        col[1] = rec[13];
+        col[2] = rec[14];
+    } else {
+        c[0] = coord_f64(__longlong_as_double((long long)load_u64_unaligned(rec)));
+        c[1] = coord_f64(__longlong_as_double((long long)load_u64_unaligned(rec + 8)));
+        c[2] = coord_f64(__longlong_as_double((long long)load_u64_unaligned(rec + 16)));
+        col[0] = rec[24];
+        col[1] = rec[25];
+        col[2] = rec[26];
+    }
+}
+
+#endif   // __CUDACC__
+
+}   // namespace oc

@@ -1,0 +1,105 @@
+// Host-side launchers of the LOD-build kernels (sm_103a).  Every launcher
+// enqueues work on `stream` and returns; errors detected on the device are
+// reported through the sticky error word `err` (see oc::kErr*).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "device_common.cuh"
+
+namespace oc {
+
+// Gridding of the finest chunking level (mapPointToGrid parameters).
+struct CloudGrid {
+    AxisGrid ax[3];
+    uint32_t grid;   // chunking grid G0
+};
+
+// Output-coordinate parameters: cloud bbox minimum and 1/scale per axis.
+struct OutParams {
+    OutAxis ax[3];
+};
+
+// One internal node to subsample.  Children are listed in slot order; each
+// child's points are records [start, start + count) of either the leaf data
+// arrays (kind 0) or the internal staging arrays (kind 1).
+struct SubNode {
+    AxisGrid ax[3];
+    uint64_t morton;
+    uint64_t cand_off;   // first candidate slot of this node in the level scratch
+    uint64_t child_start[8];
+    uint32_t child_count[8];
+    uint32_t level;
+    uint32_t p_in;       // total candidate points
+    uint32_t nchild;
+    uint32_t child_kind; // bit s set: child s lives in the staging arrays
+};
+
+enum SubMode : uint32_t {
+    kModeIntra = 1,
+    kModeInter = 2,
+    kModeRandom = 8,
+    kModeWeight = 16,
+};
+
+struct SubLevelArgs {
+    const SubNode* nodes;
+    uint32_t n_nodes;
+    uint32_t grid;        // subsampling grid S
+    uint32_t mode;        // SubMode bits (intra wins over inter, weighting only with inter)
+    uint32_t float_input;
+    uint64_t seed;
+    const uint8_t* cloud;
+    uint32_t stride;
+    const uint32_t* leaf_lut;   // final LUT (leaf part)
+    const uint8_t* leaf_rec;    // final records (leaf part)
+    const uint32_t* stage_lut;  // staging LUT of internal nodes
+    const uint8_t* stage_rec;   // staging records of internal nodes
+    uint32_t* out_lut;          // staging outputs of this level (indexed by cand_off)
+    uint8_t* out_rec;
+    uint32_t* out_points;       // per node: number of subsampled points
+    uint32_t* key_cache;        // per candidate: brick slot << 6 | bit
+    float* unit_cache;          // per candidate: cell-unit position (weighted only)
+    uint64_t* acc_best;         // per cell: selection key
+    uint64_t* acc_intra;        // per cell: packed colour sum
+    uint64_t* acc_inter;        // per cell: packed colour sum over the 3x3x3 neighbourhood
+    uint64_t* acc_w;            // per cell: 4 x fixed-point weighted sums (weighted only)
+    uint32_t* csr_count;        // per cell: candidates in the cell (weighted only)
+    uint32_t* csr_start;        // per cell
+    uint8_t* csr_pts;           // per candidate: grouped by cell (weighted only), 20 bytes each
+    OutParams out;
+    uint32_t* work_counter;
+    uint32_t* err;
+};
+
+void launch_count(const uint8_t* cloud, uint64_t n, uint32_t stride, bool float_input, const CloudGrid& g,
+                  uint32_t* pyr0, uint32_t* err, int num_sms, cudaStream_t stream);
+
+// Builds levels 1..depth of the Morton count pyramid from level 0 and counts
+// occupied cells per level into `nonzero[level]`.
+void launch_pyramid(uint32_t* pyr, const uint64_t* level_off_host, uint32_t depth, uint32_t* nonzero,
+                    cudaStream_t stream);
+
+void launch_enumerate(const uint32_t* pyr, const uint64_t* level_off_dev, uint32_t depth, uint32_t threshold,
+                      uint32_t* key, uint32_t* count, uint8_t* level, uint16_t* info, uint32_t* child_first,
+                      uint32_t cap, uint32_t* level_start, uint32_t* n_nodes, uint32_t* err, cudaStream_t stream);
+
+void launch_tag_leaves(uint32_t* pyr, const uint64_t* level_off_dev, const uint32_t* leaf_nodes, uint32_t n_leaves,
+                       const uint32_t* key, const uint8_t* level, cudaStream_t stream);
+
+void launch_distribute(const uint8_t* cloud, uint64_t n, uint32_t stride, bool float_input, const CloudGrid& g,
+                       const OutParams& out, const uint32_t* pyr, const uint64_t* level_off_dev, uint32_t depth,
+                       const uint64_t* data_idx, uint32_t* fill, uint32_t* lut, uint8_t* rec, uint32_t* err,
+                       int num_sms, cudaStream_t stream);
+
+size_t subsample_smem_bytes();
+void launch_subsample_level(const SubLevelArgs& a, int num_sms, cudaStream_t stream);
+
+// Moves staged internal-node outputs to their final (post-order) positions.
+void launch_place(const uint64_t* src_off, const uint64_t* dst_off, const uint32_t* count, uint32_t n_nodes,
+                  const uint32_t* stage_lut, const uint8_t* stage_rec, uint32_t* lut, uint8_t* rec,
+                  cudaStream_t stream);
+
+}   // namespace oc

@@ -1,0 +1,150 @@
+"""GPU parity tests: the LOD build through the C ABI (libOctreeApi.so on the
+GPU) against the CPU oracle, on seeded synthetic clouds, for every
+subsampling / colour-filtering mode and both record layouts."""
+import numpy as np
+import pytest
+
+from helpers import case_from_points, compare_results, make_case, run_gpu, run_oracle
+
+pytestmark = pytest.mark.gpu
+
+MODES = {
+    "fp_none": dict(),
+    "fp_intra": dict(intra=True),
+    "fp_inter": dict(inter=True),
+    "fp_inter_w": dict(inter=True, weighting=True),
+    "rp_none": dict(random=True),
+    "rp_intra": dict(random=True, intra=True),
+    "rp_inter": dict(random=True, inter=True),
+    "rp_inter_w": dict(random=True, inter=True, weighting=True),
+}
+
+
+@pytest.mark.parametrize("mode", sorted(MODES))
+@pytest.mark.parametrize("kind,cloud_type", [(0, 0), (1, 0), (2, 1)])
+def test_modes_small_grids(kind, cloud_type, mode):
+    case = make_case(kind, cloud_type, 120_000, seed=11 + kind, scale=0.001 if cloud_type == 0 else 0.01)
+    cfg = dict(chunk_grid=64, sub_grid=32, merge_threshold=1500, **MODES[mode])
+    ref = run_oracle(case, cfg)
+    s = run_gpu(case, cfg)
+    compare_results(ref, s)
+    s.close()
+
+
+@pytest.mark.parametrize("kind,cloud_type,mode", [(0, 0, "fp_inter"), (1, 0, "rp_intra"), (1, 0, "rp_inter_w"),
+                                                  (2, 1, "fp_inter"), (2, 1, "rp_none")])
+def test_reference_grids(kind, cloud_type, mode):
+    """Grids 512/128 and threshold 10000 as in the reference's run commands."""
+    case = make_case(kind, cloud_type, 1_500_000, seed=101 + kind, scale=0.001 if cloud_type == 0 else 0.01)
+    cfg = dict(chunk_grid=512, sub_grid=128, merge_threshold=10000, **MODES[mode])
+    ref = run_oracle(case, cfg)
+    s = run_gpu(case, cfg)
+    compare_results(ref, s)
+    s.close()
+
+
+def test_cuboid_known_answers():
+    """Known answers of the reference's 128^3 unit-cuboid tests
+    (Tests/test_merging_sparse.cpp:32-157, test_subsampling_sparse.cpp:17-33),
+    with a 15-byte record layout."""
+    case = make_case(3, 0, 128 ** 3, seed=0, scale=1.0)
+    assert case.bb_min == (0.5, 0.5, 0.5) and case.bb_max == (127.5, 127.5, 127.5)
+    cfg = dict(chunk_grid=128, sub_grid=128, merge_threshold=10000, debug=1)
+    s = run_gpu(case, cfg)
+    st = s.stats()
+    assert st["sparse_nodes"] == 2_396_745
+    for lvl, grid in enumerate([128, 64, 32, 16, 8, 4, 2, 1]):
+        counts = s.level_counts(lvl, grid)
+        assert np.all(counts == 8 ** lvl), lvl
+    hier = s.hierarchy()
+    # root: 128^3 subsampled points; 2^3 level: 64^3 each; 4^3 level: 32^3 each
+    assert hier["points"][0] == 128 ** 3
+    assert np.all(hier["points"][1:9] == 64 ** 3)
+    assert np.all(hier["points"][9:73] == 32 ** 3)
+    leaves = hier["type"] == 1
+    assert leaves.sum() == 512 and np.all(hier["points"][leaves] == 4096)
+    ref = run_oracle(case, {k: v for k, v in cfg.items() if k != "debug"})
+    compare_results(ref, s)
+    s.close()
+
+
+def test_root_below_threshold():
+    case = make_case(0, 0, 5_000, seed=3)
+    cfg = dict(chunk_grid=512, sub_grid=128, merge_threshold=10000, inter=True)
+    ref = run_oracle(case, cfg)
+    s = run_gpu(case, cfg)
+    compare_results(ref, s)
+    hier = s.hierarchy()
+    assert len(hier) == 1 and hier["type"][0] == 1 and hier["points"][0] == 5_000
+    s.close()
+
+
+def test_single_point_and_identical_points():
+    for n in (1, 40_000):
+        xyz = np.tile(np.array([[1.25, -3.5, 7.0]]), (n, 1))
+        rgb = np.full((n, 3), 200, np.uint8)
+        case = case_from_points(xyz, rgb, 0, bbox=[0, -4, 6, 2, -2, 8])
+        cfg = dict(chunk_grid=64, sub_grid=32, merge_threshold=100, intra=True)
+        ref = run_oracle(case, cfg)
+        s = run_gpu(case, cfg)
+        compare_results(ref, s)
+        s.close()
+
+
+@pytest.mark.parametrize("cloud_type", [0, 1])
+def test_cell_boundaries(cloud_type):
+    """Points on and one ulp around every cell boundary of the chunking grid and
+    of the subsampling grids, plus points on the bbox maximum."""
+    rng = np.random.default_rng(5)
+    ft = np.float32 if cloud_type == 0 else np.float64
+    lo, side, G = 3.0, 7.0, 64
+    t = side / G
+    k = np.arange(G + 1)
+    edges = (lo + k * t).astype(ft)
+    cand = np.concatenate([edges, np.nextafter(edges, ft(-np.inf)), np.nextafter(edges, ft(np.inf)),
+                           (lo + k * t / 8).astype(ft), (lo + (k + 0.5) * t / 4).astype(ft)])
+    cand = cand[(cand >= lo) & (cand <= lo + side)]
+    n = 60_000
+    xyz = np.stack([rng.choice(cand, n), rng.choice(cand, n), rng.choice(cand, n)], axis=1).astype(np.float64)
+    xyz[:100] = lo + side
+    rgb = rng.integers(0, 256, (n, 3), dtype=np.uint8)
+    case = case_from_points(xyz, rgb, cloud_type, scale=0.001, bbox=[lo, lo, lo, lo + side, lo + side, lo + side])
+    for mode in ("fp_inter", "rp_intra"):
+        cfg = dict(chunk_grid=G, sub_grid=16, merge_threshold=500, **MODES[mode])
+        ref = run_oracle(case, cfg)
+        s = run_gpu(case, cfg)
+        compare_results(ref, s)
+        s.close()
+
+
+def test_large_coordinates_double():
+    """UTM-like coordinates with a 27-byte layout: the fp32 fast path must fall
+    back to binary64 near boundaries."""
+    rng = np.random.default_rng(9)
+    n = 200_000
+    base = np.array([512345.678, 4501234.567, 250.0])
+    xyz = base + rng.random((n, 3)) * np.array([100.0, 100.0, 5.0])
+    xyz[: n // 10] = np.round(xyz[: n // 10], 2)   # coordinates on a 1 cm lattice
+    rgb = rng.integers(0, 256, (n, 3), dtype=np.uint8)
+    case = case_from_points(xyz, rgb, 1, scale=0.01)
+    cfg = dict(chunk_grid=128, sub_grid=64, merge_threshold=2000, inter=True)
+    ref = run_oracle(case, cfg)
+    s = run_gpu(case, cfg)
+    compare_results(ref, s)
+    s.close()
+
+
+def test_repeat_generate_same_session():
+    """Two generate calls on one session give identical hierarchies and records."""
+    case = make_case(0, 0, 200_000, seed=21)
+    cfg = dict(chunk_grid=128, sub_grid=64, merge_threshold=2000, random=True, inter=True)
+    s = run_gpu(case, cfg)
+    h1 = s.hierarchy().tobytes()
+    from helpers import node_sorted
+    r1, l1 = node_sorted(s.hierarchy(), s.records(), s.lut())
+    s.init()
+    s.generate()
+    assert s.hierarchy().tobytes() == h1
+    r2, l2 = node_sorted(s.hierarchy(), s.records(), s.lut())
+    assert np.array_equal(l1, l2) and r1.tobytes() == r2.tobytes()
+    s.close()
