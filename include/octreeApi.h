@@ -99,7 +99,7 @@ typedef struct OcpiStats {
     uint32_t max_leaf_points;
     float mean_leaf_points;
     float stdev_leaf_points;
-    uint32_t reserved;
+    uint32_t kernel_launches; /* kernels launched by the last ocpi_generate_octree */
 } OcpiStats;
 
 OCPI_EXPORT int ocpi_get_stats(void* session, OcpiStats* out);

@@ -184,12 +184,13 @@ void Builder::generate() {
     check_cuda(cudaMemsetAsync(err_.p, 0, 64, stream_), "memset");
     check_cuda(cudaMemsetAsync(nonzero_.p, 0, (depth_ + 1) * 4, stream_), "memset");
     stage_mark("clear");
-    launch_count(cloud_.as<uint8_t>(), cfg_.n, cfg_.stride, f32, g, pyr_.as<uint32_t>(), err_.as<uint32_t>(),
-                 num_sms_, stream_);
+    launches_ = 0;
+    launches_ += launch_count(cloud_.as<uint8_t>(), cfg_.n, cfg_.stride, f32, g, pyr_.as<uint32_t>(),
+                              err_.as<uint32_t>(), num_sms_, stream_);
     stage_mark("count");
-    launch_pyramid(pyr_.as<uint32_t>(), level_off_.data(), depth_, nonzero_.as<uint32_t>(), stream_);
+    launches_ += launch_pyramid(pyr_.as<uint32_t>(), level_off_.data(), depth_, nonzero_.as<uint32_t>(), stream_);
     stage_mark("pyramid");
-    launch_enumerate(pyr_.as<uint32_t>(), loff_.as<uint64_t>(), depth_, cfg_.threshold, key_.as<uint32_t>(),
+    launches_ += launch_enumerate(pyr_.as<uint32_t>(), loff_.as<uint64_t>(), depth_, cfg_.threshold, key_.as<uint32_t>(),
                      count_.as<uint32_t>(), level_.as<uint8_t>(), info_.as<uint16_t>(), child_first_.as<uint32_t>(),
                      node_cap_, level_start_.as<uint32_t>(), n_nodes_.as<uint32_t>(), err_.as<uint32_t>(), stream_);
     stage_mark("tree");
@@ -225,9 +226,9 @@ void Builder::generate() {
     upload_vec(data_idx_, didx, stream_);
     fill_.ensure(nodes_.size() * 4);
     check_cuda(cudaMemsetAsync(fill_.p, 0, nodes_.size() * 4, stream_), "memset");
-    launch_tag_leaves(pyr_.as<uint32_t>(), loff_.as<uint64_t>(), leaves_.as<uint32_t>(), (uint32_t)leaf_ids_.size(),
+    launches_ += launch_tag_leaves(pyr_.as<uint32_t>(), loff_.as<uint64_t>(), leaves_.as<uint32_t>(), (uint32_t)leaf_ids_.size(),
                       key_.as<uint32_t>(), level_.as<uint8_t>(), stream_);
-    launch_distribute(cloud_.as<uint8_t>(), cfg_.n, cfg_.stride, f32, g, op, pyr_.as<uint32_t>(),
+    launches_ += launch_distribute(cloud_.as<uint8_t>(), cfg_.n, cfg_.stride, f32, g, op, pyr_.as<uint32_t>(),
                       loff_.as<uint64_t>(), depth_, data_idx_.as<uint64_t>(), fill_.as<uint32_t>(),
                       lut_.as<uint32_t>(), rec_.as<uint8_t>(), err_.as<uint32_t>(), num_sms_, stream_);
     stage_mark("distribute");
@@ -314,7 +315,7 @@ void Builder::subsample() {
         const double side = cubic / std::pow(2.0, (double)(depth_ - l));   // fp_subsampling.cu:16-17
         const double t = side / S;                                         // kernel_helpers.cuh:14
         std::vector<SubNode> table(list.size());
-        uint64_t level_in = 0;
+        uint64_t level_in = 0, max_p_in = 0;
         for (size_t k = 0; k < list.size(); ++k) {
             const NodeHost& v = nodes_[list[k]];
             SubNode& sn = table[k];
@@ -341,6 +342,7 @@ void Builder::subsample() {
             if (p > 0xFFFFFFFFull) throw Error("internal node too large");
             sn.p_in = (uint32_t)p;
             sn.cand_off = level_in;
+            max_p_in = std::max<uint64_t>(max_p_in, p);
             level_in += p;
         }
         stats_.p_in += level_in;
@@ -388,7 +390,26 @@ void Builder::subsample() {
         a.out = op;
         a.work_counter = work_.as<uint32_t>();
         a.err = err_.as<uint32_t>();
-        launch_subsample_level(a, num_sms_, stream_);
+        {
+            // global brick tables: enough slots for the level's largest node
+            // at 68% load (bricks <= candidates and <= bricks of the grid)
+            uint64_t bs = (S + 3) / 4;
+            uint64_t bound = std::min<uint64_t>(max_p_in, bs * bs * bs);
+            uint64_t cap = subsample_block_size();
+            while (cap * 11 / 16 < bound + 1) cap <<= 1;
+            uint32_t shift = 32;
+            for (uint64_t c = cap; c > 1; c >>= 1) --shift;
+            size_t blocks = (size_t)std::min<uint64_t>(list.size(), (uint64_t)num_sms_);
+            g_key_.ensure(blocks * cap * 4);
+            g_mask_.ensure(blocks * cap * 8);
+            g_base_.ensure(blocks * cap * 4);
+            a.global_key = g_key_.as<uint32_t>();
+            a.global_mask = g_mask_.as<uint64_t>();
+            a.global_base = g_base_.as<uint32_t>();
+            a.global_cap = (uint32_t)cap;
+            a.global_shift = shift;
+        }
+        launches_ += launch_subsample_level(a, num_sms_, stream_);
         check_cuda(cudaGetLastError(), "subsample launch");
         std::vector<uint32_t> pts(list.size());
         check_cuda(cudaMemcpyAsync(pts.data(), out_points_.p, pts.size() * 4, cudaMemcpyDeviceToHost, stream_), "D2H");
@@ -436,7 +457,7 @@ void Builder::place_internal() {
     upload_vec(place_src_, src, stream_);
     upload_vec(place_dst_, dst, stream_);
     upload_vec(place_cnt_, cnt, stream_);
-    launch_place(place_src_.as<uint64_t>(), place_dst_.as<uint64_t>(), place_cnt_.as<uint32_t>(), (uint32_t)cnt.size(),
+    launches_ += launch_place(place_src_.as<uint64_t>(), place_dst_.as<uint64_t>(), place_cnt_.as<uint32_t>(), (uint32_t)cnt.size(),
                  stage_lut_.as<uint32_t>(), stage_rec_.as<uint8_t>(), lut_.as<uint32_t>(), rec_.as<uint8_t>(),
                  stream_);
 }
@@ -451,6 +472,7 @@ void Builder::compute_stats() {
     S.points_total = (uint64_t)cfg_.n + p_out_;
     S.out_capacity = (uint64_t)((float)cfg_.n * cfg_.output_factor);   // point_cloud.cuh:24
     S.dense_nodes = (uint32_t)level_off_[depth_ + 1];
+    S.kernel_launches = launches_;
     std::vector<uint32_t> nz(depth_ + 1);
     check_cuda(cudaMemcpy(nz.data(), nonzero_.p, nz.size() * 4, cudaMemcpyDeviceToHost), "D2H");
     S.sparse_nodes = 0;

@@ -76,6 +76,7 @@ struct Stats {
     uint32_t depth = 0, tree_nodes = 0, leaf_nodes = 0, internal_nodes = 0, sparse_nodes = 0, dense_nodes = 0;
     uint32_t max_leaf_depth = 0, min_leaf_points = 0, max_leaf_points = 0;
     float mean_leaf_points = 0.f, stdev_leaf_points = 0.f;
+    uint32_t kernel_launches = 0;   // kernels launched by the last generate
 };
 
 class Builder {
@@ -128,6 +129,8 @@ private:
     DevBuf sub_nodes_, out_points_, work_;
     DevBuf key_cache_, unit_cache_, acc_best_, acc_intra_, acc_w_, csr_count_, csr_start_, csr_pts_;
     DevBuf place_src_, place_dst_, place_cnt_;
+    DevBuf g_key_, g_mask_, g_base_;   // per-block global brick tables
+    uint32_t launches_ = 0;
 
     std::vector<NodeHost> nodes_;
     std::vector<uint32_t> leaf_ids_;

@@ -341,12 +341,12 @@ static size_t tile_smem(uint32_t stride) {
     return (size_t)kTilePoints * stride + 64;
 }
 
-void launch_count(const uint8_t* cloud, uint64_t n, uint32_t stride, bool float_input, const CloudGrid& g,
+int launch_count(const uint8_t* cloud, uint64_t n, uint32_t stride, bool float_input, const CloudGrid& g,
                   uint32_t* pyr0, uint32_t* err, int num_sms, cudaStream_t stream) {
     size_t smem = tile_smem(stride);
     uint64_t tiles = (n + kTilePoints - 1) / kTilePoints;
     int grid = (int)std::min<uint64_t>(tiles, (uint64_t)num_sms * 4);
-    if (grid == 0) return;
+    if (grid == 0) return 0;
     if (float_input) {
         cudaFuncSetAttribute(k_count<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_count<true><<<grid, kTileThreads, smem, stream>>>(cloud, n, stride, g, pyr0, err);
@@ -354,11 +354,14 @@ void launch_count(const uint8_t* cloud, uint64_t n, uint32_t stride, bool float_
         cudaFuncSetAttribute(k_count<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_count<false><<<grid, kTileThreads, smem, stream>>>(cloud, n, stride, g, pyr0, err);
     }
+    return 1;
 }
 
-void launch_pyramid(uint32_t* pyr, const uint64_t* loff, uint32_t depth, uint32_t* nonzero, cudaStream_t stream) {
+int launch_pyramid(uint32_t* pyr, const uint64_t* loff, uint32_t depth, uint32_t* nonzero, cudaStream_t stream) {
     uint32_t l = 0;
+    int launches = 1;
     while (l < depth) {
+        ++launches;
         if (l + 2 <= depth) {
             uint64_t n2 = loff[l + 3 <= depth + 1 ? l + 3 : depth + 1] - loff[l + 2];
             n2 = 0;
@@ -378,29 +381,32 @@ void launch_pyramid(uint32_t* pyr, const uint64_t* loff, uint32_t depth, uint32_
         }
     }
     k_count_root<<<1, 32, 0, stream>>>(pyr + loff[depth], nonzero + depth);
+    return launches;
 }
 
-void launch_enumerate(const uint32_t* pyr, const uint64_t* loff_dev, uint32_t depth, uint32_t threshold, uint32_t* key,
+int launch_enumerate(const uint32_t* pyr, const uint64_t* loff_dev, uint32_t depth, uint32_t threshold, uint32_t* key,
                       uint32_t* count, uint8_t* level, uint16_t* info, uint32_t* child_first, uint32_t cap,
                       uint32_t* level_start, uint32_t* n_nodes, uint32_t* err, cudaStream_t stream) {
     k_enumerate<<<1, 1024, 0, stream>>>(pyr, loff_dev, depth, threshold, key, count, level, info, child_first, cap,
                                         level_start, n_nodes, err);
+    return 1;
 }
 
-void launch_tag_leaves(uint32_t* pyr, const uint64_t* loff_dev, const uint32_t* leaves, uint32_t n_leaves,
+int launch_tag_leaves(uint32_t* pyr, const uint64_t* loff_dev, const uint32_t* leaves, uint32_t n_leaves,
                        const uint32_t* key, const uint8_t* level, cudaStream_t stream) {
-    if (!n_leaves) return;
+    if (!n_leaves) return 0;
     k_tag_leaves<<<(n_leaves + 255) / 256, 256, 0, stream>>>(pyr, loff_dev, leaves, n_leaves, key, level);
+    return 1;
 }
 
-void launch_distribute(const uint8_t* cloud, uint64_t n, uint32_t stride, bool float_input, const CloudGrid& g,
+int launch_distribute(const uint8_t* cloud, uint64_t n, uint32_t stride, bool float_input, const CloudGrid& g,
                        const OutParams& out, const uint32_t* pyr, const uint64_t* loff_dev, uint32_t depth,
                        const uint64_t* data_idx, uint32_t* fill, uint32_t* lut, uint8_t* rec, uint32_t* err,
                        int num_sms, cudaStream_t stream) {
     size_t smem = tile_smem(stride);
     uint64_t tiles = (n + kTilePoints - 1) / kTilePoints;
     int grid = (int)std::min<uint64_t>(tiles, (uint64_t)num_sms * 4);
-    if (grid == 0) return;
+    if (grid == 0) return 0;
     if (float_input) {
         cudaFuncSetAttribute(k_distribute<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_distribute<true><<<grid, kTileThreads, smem, stream>>>(cloud, n, stride, g, out, pyr, loff_dev, depth,
@@ -410,14 +416,16 @@ void launch_distribute(const uint8_t* cloud, uint64_t n, uint32_t stride, bool f
         k_distribute<false><<<grid, kTileThreads, smem, stream>>>(cloud, n, stride, g, out, pyr, loff_dev, depth,
                                                                   data_idx, fill, lut, rec, err);
     }
+    return 1;
 }
 
-void launch_place(const uint64_t* src_off, const uint64_t* dst_off, const uint32_t* count, uint32_t n_nodes,
+int launch_place(const uint64_t* src_off, const uint64_t* dst_off, const uint32_t* count, uint32_t n_nodes,
                   const uint32_t* stage_lut, const uint8_t* stage_rec, uint32_t* lut, uint8_t* rec,
                   cudaStream_t stream) {
-    if (!n_nodes) return;
+    if (!n_nodes) return 0;
     unsigned grid = n_nodes < 4096 ? n_nodes : 4096;
     k_place<<<grid, 256, 0, stream>>>(src_off, dst_off, count, n_nodes, stage_lut, stage_rec, lut, rec);
+    return 1;
 }
 
 }   // namespace oc

@@ -34,53 +34,61 @@ namespace oc {
 namespace {
 
 constexpr int kSubThreads = 1024;
-constexpr uint32_t kBrickSlots = 8192;   // shared hash capacity (bricks)
-constexpr uint32_t kSlotsPerThread = kBrickSlots / kSubThreads;
-
-__device__ __forceinline__ uint32_t brick_hash(uint32_t b1) {
-    return (b1 * 2654435761u) >> (32 - 13);
-}
-
-__device__ __forceinline__ uint32_t brick_insert(uint32_t* keys, uint32_t b1, uint32_t* err) {
-    volatile uint32_t* vk = keys;
-    uint32_t h = brick_hash(b1);
-    for (uint32_t probe = 0; probe < kBrickSlots; ++probe) {
-        uint32_t cur = vk[h];
-        if (cur == b1) return h;
-        if (cur == 0) {
-            uint32_t old = atomicCAS(&keys[h], 0u, b1);
-            if (old == 0 || old == b1) return h;
-        }
-        h = (h + 1) & (kBrickSlots - 1);
-    }
-    atomicOr(err, kErrProbe);
-    return kBrickSlots;
-}
-
-__device__ __forceinline__ int brick_find(const uint32_t* keys, uint32_t b1) {
-    uint32_t h = brick_hash(b1);
-    for (uint32_t probe = 0; probe < kBrickSlots; ++probe) {
-        uint32_t cur = keys[h];
-        if (cur == b1) return (int)h;
-        if (cur == 0) return -1;
-        h = (h + 1) & (kBrickSlots - 1);
-    }
-    return -1;
-}
+constexpr uint32_t kBrickSlots = 8192;    // shared-memory brick table capacity
+constexpr uint32_t kBrickShift = 32 - 13;
 
 struct BrickMap {
     uint32_t* key;    // brick id + 1, 0 = empty
     uint64_t* mask;   // occupied cells of the brick (bit = x | y<<2 | z<<4)
     uint32_t* base;   // rank of the brick's first cell
+    uint32_t cap;     // slots (power of two, multiple of the block size)
+    uint32_t shift;   // 32 - log2(cap)
     uint32_t bs;      // bricks per axis
     uint32_t grid;    // S
 };
+
+__device__ __forceinline__ uint32_t brick_hash(const BrickMap& m, uint32_t b1) {
+    return (b1 * 2654435761u) >> m.shift;
+}
+
+// Inserts brick b1 (id + 1); returns its slot (cap on failure) and whether
+// this call claimed the slot.
+__device__ __forceinline__ uint32_t brick_insert(const BrickMap& m, uint32_t b1, bool& fresh) {
+    volatile uint32_t* vk = m.key;
+    uint32_t h = brick_hash(m, b1);
+    fresh = false;
+    for (uint32_t probe = 0; probe < m.cap; ++probe) {
+        uint32_t cur = vk[h];
+        if (cur == b1) return h;
+        if (cur == 0) {
+            uint32_t old = atomicCAS(&m.key[h], 0u, b1);
+            if (old == 0) {
+                fresh = true;
+                return h;
+            }
+            if (old == b1) return h;
+        }
+        h = (h + 1) & (m.cap - 1);
+    }
+    return m.cap;
+}
+
+__device__ __forceinline__ int brick_find(const BrickMap& m, uint32_t b1) {
+    uint32_t h = brick_hash(m, b1);
+    for (uint32_t probe = 0; probe < m.cap; ++probe) {
+        uint32_t cur = m.key[h];
+        if (cur == b1) return (int)h;
+        if (cur == 0) return -1;
+        h = (h + 1) & (m.cap - 1);
+    }
+    return -1;
+}
 
 // Rank of cell (x, y, z) or -1 when unoccupied / outside the grid.
 __device__ __forceinline__ int cell_rank(const BrickMap& m, int x, int y, int z) {
     if (x < 0 || y < 0 || z < 0 || x >= (int)m.grid || y >= (int)m.grid || z >= (int)m.grid) return -1;
     uint32_t b = ((uint32_t)x >> 2) + m.bs * (((uint32_t)y >> 2) + m.bs * ((uint32_t)z >> 2));
-    int s = brick_find(m.key, b + 1);
+    int s = brick_find(m, b + 1);
     if (s < 0) return -1;
     uint32_t bit = (x & 3) | ((y & 3) << 2) | ((z & 3) << 4);
     uint64_t mk = m.mask[s];
@@ -136,12 +144,22 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
     extern __shared__ uint64_t dyn[];
     __shared__ NodeShared ns;
     __shared__ uint32_t warp_sums[32];
-    BrickMap bm;
-    bm.mask = dyn;
-    bm.key = reinterpret_cast<uint32_t*>(dyn + kBrickSlots);
-    bm.base = bm.key + kBrickSlots;
-    bm.grid = a.grid;
-    bm.bs = (a.grid + 3) >> 2;
+    __shared__ uint32_t s_bricks, s_overflow;
+    BrickMap sm_map;
+    sm_map.mask = dyn;
+    sm_map.key = reinterpret_cast<uint32_t*>(dyn + kBrickSlots);
+    sm_map.base = sm_map.key + kBrickSlots;
+    sm_map.cap = kBrickSlots;
+    sm_map.shift = kBrickShift;
+    sm_map.grid = a.grid;
+    sm_map.bs = (a.grid + 3) >> 2;
+    // per-block brick table in global memory for nodes that outgrow shared memory
+    BrickMap gl_map = sm_map;
+    gl_map.cap = a.global_cap;
+    gl_map.shift = a.global_shift;
+    gl_map.mask = a.global_mask + (uint64_t)blockIdx.x * a.global_cap;
+    gl_map.key = a.global_key + (uint64_t)blockIdx.x * a.global_cap;
+    gl_map.base = a.global_base + (uint64_t)blockIdx.x * a.global_cap;
 
     const bool intra = (a.mode & kModeIntra) != 0;
     const bool inter = !intra && (a.mode & kModeInter) != 0;
@@ -167,63 +185,88 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
             }
             ns.prefix[nd.nchild] = p;
         }
-        for (uint32_t i = threadIdx.x; i < kBrickSlots; i += blockDim.x) {
-            bm.key[i] = 0;
-            bm.mask[i] = 0;
-        }
         const AxisGrid ax0 = nd.ax[0], ax1 = nd.ax[1], ax2 = nd.ax[2];
         const uint32_t p_in = nd.p_in;
         const uint64_t off = nd.cand_off;
-        __syncthreads();
+        BrickMap bm = sm_map;
 
-        // ---- pass A: cells and occupancy
-        for (uint32_t j = threadIdx.x; j < p_in; j += blockDim.x) {
-            uint32_t c;
-            uint64_t pos;
-            locate(ns, j, c, pos);
-            bool staged = (ns.kind >> c) & 1u;
-            uint32_t idx = staged ? a.stage_lut[pos] : a.leaf_lut[pos];
-            Coord co[3];
-            uint32_t col[3];
-            load_point<kF32>(a.cloud + (uint64_t)idx * a.stride, co, col);
-            float ux, uy, uz;
-            int ix = axis_cell<kF32>(co[0], ax0, a.grid, ux);
-            int iy = axis_cell<kF32>(co[1], ax1, a.grid, uy);
-            int iz = axis_cell<kF32>(co[2], ax2, a.grid, uz);
-            if ((ix | iy | iz) < 0) {
-                atomicOr(a.err, kErrBelowBox);
-                ix = max(ix, 0);
-                iy = max(iy, 0);
-                iz = max(iz, 0);
+        // ---- pass A: cells and occupancy.  A node whose bricks exceed 70% of
+        // the shared table is redone with the block's global-memory table.
+        for (int attempt = 0; attempt < 2; ++attempt) {
+            for (uint32_t i = threadIdx.x; i < bm.cap; i += blockDim.x) {
+                bm.key[i] = 0;
+                bm.mask[i] = 0;
             }
-            uint32_t b = ((uint32_t)ix >> 2) + bm.bs * (((uint32_t)iy >> 2) + bm.bs * ((uint32_t)iz >> 2));
-            uint32_t bit = (ix & 3) | ((iy & 3) << 2) | ((iz & 3) << 4);
-            uint32_t slot = brick_insert(bm.key, b + 1, a.err);
-            if (slot < kBrickSlots) atomicOr(reinterpret_cast<unsigned long long*>(&bm.mask[slot]), 1ull << bit);
-            a.key_cache[off + j] = (slot << 6) | bit;
-            if (weighted) {
-                a.unit_cache[(off + j) * 3 + 0] = ux;
-                a.unit_cache[(off + j) * 3 + 1] = uy;
-                a.unit_cache[(off + j) * 3 + 2] = uz;
+            if (threadIdx.x == 0) {
+                s_bricks = 0;
+                s_overflow = 0;
             }
+            __syncthreads();
+            const uint32_t limit = bm.cap - (bm.cap >> 2) - (bm.cap >> 4);
+            for (uint32_t j = threadIdx.x; j < p_in; j += blockDim.x) {
+                if (*(volatile uint32_t*)&s_overflow) break;
+                uint32_t c;
+                uint64_t pos;
+                locate(ns, j, c, pos);
+                bool staged = (ns.kind >> c) & 1u;
+                uint32_t idx = staged ? a.stage_lut[pos] : a.leaf_lut[pos];
+                Coord co[3];
+                uint32_t col[3];
+                load_point<kF32>(a.cloud + (uint64_t)idx * a.stride, co, col);
+                float ux, uy, uz;
+                int ix = axis_cell<kF32>(co[0], ax0, a.grid, ux);
+                int iy = axis_cell<kF32>(co[1], ax1, a.grid, uy);
+                int iz = axis_cell<kF32>(co[2], ax2, a.grid, uz);
+                if ((ix | iy | iz) < 0) {
+                    atomicOr(a.err, kErrBelowBox);
+                    ix = max(ix, 0);
+                    iy = max(iy, 0);
+                    iz = max(iz, 0);
+                }
+                uint32_t b = ((uint32_t)ix >> 2) + bm.bs * (((uint32_t)iy >> 2) + bm.bs * ((uint32_t)iz >> 2));
+                uint32_t bit = (ix & 3) | ((iy & 3) << 2) | ((iz & 3) << 4);
+                bool fresh;
+                uint32_t slot = brick_insert(bm, b + 1, fresh);
+                if (fresh && atomicAdd(&s_bricks, 1u) + 1 >= limit) s_overflow = 1;
+                if (slot >= bm.cap) {
+                    s_overflow = 1;
+                    break;
+                }
+                atomicOr(reinterpret_cast<unsigned long long*>(&bm.mask[slot]), 1ull << bit);
+                a.key_cache[off + j] = (slot << 6) | bit;
+                if (weighted) {
+                    a.unit_cache[(off + j) * 3 + 0] = ux;
+                    a.unit_cache[(off + j) * 3 + 1] = uy;
+                    a.unit_cache[(off + j) * 3 + 2] = uz;
+                }
+            }
+            __syncthreads();
+            if (!s_overflow) break;
+            if (attempt == 1 || bm.key == gl_map.key) {
+                if (threadIdx.x == 0) atomicOr(a.err, kErrProbe);
+                break;
+            }
+            bm = gl_map;
+            __syncthreads();
         }
+        const bool failed = s_overflow != 0;
         __syncthreads();
+        if (failed) {
+            if (threadIdx.x == 0) a.out_points[ni] = 0;
+            continue;
+        }
 
-        // ---- ranks of occupied cells
+        // ---- ranks of occupied cells (each thread scans a run of slots)
         {
-            uint32_t local[kSlotsPerThread];
+            const uint32_t per = bm.cap / blockDim.x;
+            const uint32_t first = threadIdx.x * per;
             uint32_t sum = 0;
-#pragma unroll
-            for (uint32_t k = 0; k < kSlotsPerThread; ++k) {
-                local[k] = (uint32_t)__popcll(bm.mask[threadIdx.x * kSlotsPerThread + k]);
-                sum += local[k];
-            }
+            for (uint32_t k = 0; k < per; ++k) sum += (uint32_t)__popcll(bm.mask[first + k]);
             uint32_t total;
             uint32_t pre = block_exclusive_scan(sum, warp_sums, total);
-#pragma unroll
-            for (uint32_t k = 0; k < kSlotsPerThread; ++k) {
-                bm.base[threadIdx.x * kSlotsPerThread + k] = pre;
-                pre += local[k];
+            for (uint32_t k = 0; k < per; ++k) {
+                bm.base[first + k] = pre;
+                pre += (uint32_t)__popcll(bm.mask[first + k]);
             }
             if (threadIdx.x == 0) ns.cells = total;
         }
@@ -240,7 +283,7 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
         for (uint32_t j = threadIdx.x; j < p_in; j += blockDim.x) {
             uint32_t kc = a.key_cache[off + j];
             uint32_t slot = kc >> 6, bit = kc & 63;
-            if (slot >= kBrickSlots) continue;
+            if (slot >= bm.cap) continue;
             uint32_t rank = bm.base[slot] + (uint32_t)__popcll(bm.mask[slot] & ((1ull << bit) - 1ull));
             uint32_t c;
             uint64_t pos;
@@ -277,7 +320,7 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
             for (uint32_t j = threadIdx.x; j < p_in; j += blockDim.x) {
                 uint32_t kc = a.key_cache[off + j];
                 uint32_t slot = kc >> 6, bit = kc & 63;
-                if (slot >= kBrickSlots) continue;
+                if (slot >= bm.cap) continue;
                 uint32_t rank = bm.base[slot] + (uint32_t)__popcll(bm.mask[slot] & ((1ull << bit) - 1ull));
                 uint32_t p = a.csr_start[off + rank] + atomicAdd(&a.csr_count[off + rank], 1u);
                 uint32_t c;
@@ -298,22 +341,26 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
         // ---- emit one record per occupied cell
         for (uint32_t r = threadIdx.x; r < cells; r += blockDim.x) {
             // slot holding rank r: last slot with base <= r and a non-empty mask
-            uint32_t lo = 0, hi = kBrickSlots - 1;
+            uint32_t lo = 0, hi = bm.cap - 1;
             while (lo < hi) {
                 uint32_t mid = (lo + hi + 1) >> 1;
                 if (bm.base[mid] <= r) lo = mid;
                 else hi = mid - 1;
             }
             uint32_t slot = lo;
-            while (bm.mask[slot] == 0 || bm.base[slot] > r) --slot;
+            while (slot > 0 && (bm.mask[slot] == 0 || bm.base[slot] > r)) --slot;
             uint64_t mk = bm.mask[slot];
             uint32_t want = r - bm.base[slot];
             uint32_t bit = 0;
-            for (uint32_t seen = 0;; ++bit) {
+            for (uint32_t seen = 0; bit < 64; ++bit) {
                 if ((mk >> bit) & 1ull) {
                     if (seen == want) break;
                     ++seen;
                 }
+            }
+            if (bit >= 64) {
+                atomicOr(a.err, kErrProbe);
+                bit = 0;
             }
             uint32_t brick = bm.key[slot] - 1;
             int bx = (int)(brick % bm.bs), by = (int)((brick / bm.bs) % bm.bs), bz = (int)(brick / (bm.bs * bm.bs));
@@ -374,12 +421,16 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
 
 }   // namespace
 
+uint32_t subsample_block_size() {
+    return kSubThreads;
+}
+
 size_t subsample_smem_bytes() {
     return (size_t)kBrickSlots * (8 + 4 + 4);
 }
 
-void launch_subsample_level(const SubLevelArgs& a, int num_sms, cudaStream_t stream) {
-    if (!a.n_nodes) return;
+int launch_subsample_level(const SubLevelArgs& a, int num_sms, cudaStream_t stream) {
+    if (!a.n_nodes) return 0;
     size_t smem = subsample_smem_bytes();
     int grid = (int)std::min<uint32_t>(a.n_nodes, (uint32_t)num_sms);
     if (a.float_input) {
@@ -389,6 +440,7 @@ void launch_subsample_level(const SubLevelArgs& a, int num_sms, cudaStream_t str
         cudaFuncSetAttribute(k_subsample<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_subsample<false><<<grid, kSubThreads, smem, stream>>>(a);
     }
+    return 1;
 }
 
 }   // namespace oc

@@ -72,33 +72,40 @@ struct SubLevelArgs {
     OutParams out;
     uint32_t* work_counter;
     uint32_t* err;
+    // per-block brick tables in global memory (gridDim.x * global_cap slots)
+    uint32_t* global_key;
+    uint64_t* global_mask;
+    uint32_t* global_base;
+    uint32_t global_cap;     // power of two, >= 1024
+    uint32_t global_shift;   // 32 - log2(global_cap)
 };
 
-void launch_count(const uint8_t* cloud, uint64_t n, uint32_t stride, bool float_input, const CloudGrid& g,
+int launch_count(const uint8_t* cloud, uint64_t n, uint32_t stride, bool float_input, const CloudGrid& g,
                   uint32_t* pyr0, uint32_t* err, int num_sms, cudaStream_t stream);
 
 // Builds levels 1..depth of the Morton count pyramid from level 0 and counts
 // occupied cells per level into `nonzero[level]`.
-void launch_pyramid(uint32_t* pyr, const uint64_t* level_off_host, uint32_t depth, uint32_t* nonzero,
+int launch_pyramid(uint32_t* pyr, const uint64_t* level_off_host, uint32_t depth, uint32_t* nonzero,
                     cudaStream_t stream);
 
-void launch_enumerate(const uint32_t* pyr, const uint64_t* level_off_dev, uint32_t depth, uint32_t threshold,
+int launch_enumerate(const uint32_t* pyr, const uint64_t* level_off_dev, uint32_t depth, uint32_t threshold,
                       uint32_t* key, uint32_t* count, uint8_t* level, uint16_t* info, uint32_t* child_first,
                       uint32_t cap, uint32_t* level_start, uint32_t* n_nodes, uint32_t* err, cudaStream_t stream);
 
-void launch_tag_leaves(uint32_t* pyr, const uint64_t* level_off_dev, const uint32_t* leaf_nodes, uint32_t n_leaves,
+int launch_tag_leaves(uint32_t* pyr, const uint64_t* level_off_dev, const uint32_t* leaf_nodes, uint32_t n_leaves,
                        const uint32_t* key, const uint8_t* level, cudaStream_t stream);
 
-void launch_distribute(const uint8_t* cloud, uint64_t n, uint32_t stride, bool float_input, const CloudGrid& g,
+int launch_distribute(const uint8_t* cloud, uint64_t n, uint32_t stride, bool float_input, const CloudGrid& g,
                        const OutParams& out, const uint32_t* pyr, const uint64_t* level_off_dev, uint32_t depth,
                        const uint64_t* data_idx, uint32_t* fill, uint32_t* lut, uint8_t* rec, uint32_t* err,
                        int num_sms, cudaStream_t stream);
 
 size_t subsample_smem_bytes();
-void launch_subsample_level(const SubLevelArgs& a, int num_sms, cudaStream_t stream);
+uint32_t subsample_block_size();
+int launch_subsample_level(const SubLevelArgs& a, int num_sms, cudaStream_t stream);
 
 // Moves staged internal-node outputs to their final (post-order) positions.
-void launch_place(const uint64_t* src_off, const uint64_t* dst_off, const uint32_t* count, uint32_t n_nodes,
+int launch_place(const uint64_t* src_off, const uint64_t* dst_off, const uint32_t* count, uint32_t n_nodes,
                   const uint32_t* stage_lut, const uint8_t* stage_rec, uint32_t* lut, uint8_t* rec,
                   cudaStream_t stream);
 

@@ -255,6 +255,7 @@ int ocpi_get_stats(void* session, OcpiStats* out) {
         o.max_leaf_points = S.max_leaf_points;
         o.mean_leaf_points = S.mean_leaf_points;
         o.stdev_leaf_points = S.stdev_leaf_points;
+        o.kernel_launches = S.kernel_launches;
         *out = o;
     });
 }

@@ -17,7 +17,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libOctreeApi.so")
 SYNTH_PATH = os.path.join(HERE, "libocsynth.so")
 
-# The 19 entry points of the reference API (OctreeApi/include/octreeApi.h:42-72).
+# The 18 entry points of the reference API (OctreeApi/include/octreeApi.h:42-72).
 REFERENCE_SYMBOLS = [
     "ocpi_create_session", "ocpi_destroy_session", "ocpi_set_logging_level",
     "ocpi_set_cloud_type", "ocpi_set_cloud_point_amount", "ocpi_set_cloud_data_stride",
@@ -49,7 +49,7 @@ class OcpiStats(ctypes.Structure):
         ("leaf_nodes", ctypes.c_uint32), ("internal_nodes", ctypes.c_uint32), ("sparse_nodes", ctypes.c_uint32),
         ("dense_nodes", ctypes.c_uint32), ("max_leaf_depth", ctypes.c_uint32), ("min_leaf_points", ctypes.c_uint32),
         ("max_leaf_points", ctypes.c_uint32), ("mean_leaf_points", ctypes.c_float),
-        ("stdev_leaf_points", ctypes.c_float), ("reserved", ctypes.c_uint32),
+        ("stdev_leaf_points", ctypes.c_float), ("kernel_launches", ctypes.c_uint32),
     ]
 
     def as_dict(self):
