@@ -270,8 +270,9 @@ def main():
     # ---- roofline of the dominant stage
     peak, peak_kind = peaks()
     sb = stage_bytes(st, n, STRIDE, stage_avg)
+    sub_ms = sum(v for k, v in stage_avg.items() if k.startswith("sub_l"))
     stage_ms = {"count": stage_avg.get("count", 0), "distribute": stage_avg.get("distribute", 0),
-                "subsample": stage_avg.get("subsample", 0)}
+                "subsample": sub_ms}
     dom = max(stage_ms, key=stage_ms.get)
     achieved = sb[dom] / (stage_ms[dom] * 1e-3) / 1e9
     traffic = None

@@ -40,6 +40,9 @@ def _run(cmd):
     return r.stdout + r.stderr
 
 
+EXTRA_NVCC = os.environ.get("OC_EXTRA_NVCC", "").split()
+
+
 def _compile(src, verbose_ptxas=False):
     path = os.path.join(CSRC, src)
     obj = os.path.join(BUILD, src + ".o")
@@ -47,7 +50,7 @@ def _compile(src, verbose_ptxas=False):
     if _newer(obj, deps) and not verbose_ptxas:
         return obj, ""
     if src.endswith(".cu"):
-        cmd = [NVCC, *ARCH, "-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
+        cmd = [NVCC, *ARCH, *EXTRA_NVCC, "-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
                "-Xcompiler", "-fvisibility=hidden", "-c", path, "-o", obj]
         if verbose_ptxas:
             cmd.insert(1, "-Xptxas=-v")

@@ -358,7 +358,7 @@ void Builder::subsample() {
         }
         uint64_t need = stage_used_ + level_in;
         stage_lut_.ensure_keep(need * 4, stage_used_ * 4, stream_);
-        stage_rec_.ensure_keep(need * 18, stage_used_ * 18, stream_);
+        stage_rec_.ensure_keep(need * 18 + 64, stage_used_ * 18, stream_);
         upload_vec(sub_nodes_, table, stream_);
         out_points_.ensure(list.size() * 4);
         work_.ensure(4);
@@ -395,7 +395,7 @@ void Builder::subsample() {
             // at 68% load (bricks <= candidates and <= bricks of the grid)
             uint64_t bs = (S + 3) / 4;
             uint64_t bound = std::min<uint64_t>(max_p_in, bs * bs * bs);
-            uint64_t cap = subsample_block_size();
+            uint64_t cap = 1024;
             while (cap * 11 / 16 < bound + 1) cap <<= 1;
             uint32_t shift = 32;
             for (uint64_t c = cap; c > 1; c >>= 1) --shift;
@@ -409,7 +409,12 @@ void Builder::subsample() {
             a.global_cap = (uint32_t)cap;
             a.global_shift = shift;
         }
+        char mark[32];
+        std::snprintf(mark, sizeof mark, "sub_host_l%u", l);
+        stage_mark(mark);
         launches_ += launch_subsample_level(a, num_sms_, stream_);
+        std::snprintf(mark, sizeof mark, "sub_l%u", l);
+        stage_mark(mark);
         check_cuda(cudaGetLastError(), "subsample launch");
         std::vector<uint32_t> pts(list.size());
         check_cuda(cudaMemcpyAsync(pts.data(), out_points_.p, pts.size() * 4, cudaMemcpyDeviceToHost, stream_), "D2H");
@@ -457,9 +462,10 @@ void Builder::place_internal() {
     upload_vec(place_src_, src, stream_);
     upload_vec(place_dst_, dst, stream_);
     upload_vec(place_cnt_, cnt, stream_);
-    launches_ += launch_place(place_src_.as<uint64_t>(), place_dst_.as<uint64_t>(), place_cnt_.as<uint32_t>(), (uint32_t)cnt.size(),
-                 stage_lut_.as<uint32_t>(), stage_rec_.as<uint8_t>(), lut_.as<uint32_t>(), rec_.as<uint8_t>(),
-                 stream_);
+    place_count_ = cnt.size();
+    launches_ += launch_place(place_src_.as<uint64_t>(), place_dst_.as<uint64_t>(), place_cnt_.as<uint32_t>(),
+                              (uint32_t)cnt.size(), stage_rec_.as<uint8_t>(), rec_.as<uint8_t>(), stream_);
+    lut_placed_ = false;
 }
 
 void Builder::compute_stats() {
@@ -533,7 +539,15 @@ void Builder::copy_records(uint8_t* out) const {
     check_cuda(cudaMemcpy(out, rec_.p, stats_.points_total * 18, cudaMemcpyDeviceToHost), "D2H records");
 }
 
-void Builder::copy_lut(uint32_t* out) const {
+void Builder::copy_lut(uint32_t* out) {
+    // internal-node cloud indices are moved to their final positions on demand
+    if (!lut_placed_) {
+        launch_place_lut(place_src_.as<uint64_t>(), place_dst_.as<uint64_t>(), place_cnt_.as<uint32_t>(),
+                         (uint32_t)(place_cnt_.bytes ? place_count_ : 0), stage_lut_.as<uint32_t>(), lut_.as<uint32_t>(),
+                         stream_);
+        check_cuda(cudaStreamSynchronize(stream_), "place lut");
+        lut_placed_ = true;
+    }
     check_cuda(cudaMemcpy(out, lut_.p, stats_.points_total * 4, cudaMemcpyDeviceToHost), "D2H lut");
 }
 

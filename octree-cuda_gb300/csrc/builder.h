@@ -97,7 +97,7 @@ public:
     const std::vector<NodeHost>& nodes() const { return nodes_; }
     std::vector<uint8_t> hierarchy() const;
     void copy_records(uint8_t* out) const;
-    void copy_lut(uint32_t* out) const;
+    void copy_lut(uint32_t* out);
     bool level_counts(uint32_t level, uint32_t* out) const;
     const std::vector<std::pair<std::string, double>>& timings() const { return timings_; }
     cudaStream_t stream() const { return stream_; }
@@ -131,6 +131,8 @@ private:
     DevBuf place_src_, place_dst_, place_cnt_;
     DevBuf g_key_, g_mask_, g_base_;   // per-block global brick tables
     uint32_t launches_ = 0;
+    size_t place_count_ = 0;
+    bool lut_placed_ = false;
 
     std::vector<NodeHost> nodes_;
     std::vector<uint32_t> leaf_ids_;

@@ -334,31 +334,42 @@ __device__ __forceinline__ void store_record(uint8_t* base, uint64_t pos, int32_
     p[8] = b;
 }
 
-// Unaligned little-endian loads of a cloud record (15- or 27-byte stride).
-__device__ __forceinline__ uint32_t load_u32_unaligned(const uint8_t* p) {
-    return (uint32_t)p[0] | ((uint32_t)p[1] << 8) | ((uint32_t)p[2] << 16) | ((uint32_t)p[3] << 24);
-}
-
-__device__ __forceinline__ uint64_t load_u64_unaligned(const uint8_t* p) {
-    return (uint64_t)load_u32_unaligned(p) | ((uint64_t)load_u32_unaligned(p + 4) << 32);
+// Record loads.  A 15- or 27-byte record starts at any byte; it is read as
+// the 8-byte-aligned words that cover it (3 words for 15 bytes, 5 for 27) and
+// realigned with funnel shifts.  Memory (global or shared) must be readable up
+// to 16 bytes past the record: the cloud buffer and the staging tiles are
+// padded for that.
+__device__ __forceinline__ uint64_t shr128(uint64_t lo, uint64_t hi, uint32_t s) {
+    uint32_t a = (uint32_t)lo, b = (uint32_t)(lo >> 32), c = (uint32_t)hi;
+    uint32_t r0 = __funnelshift_r(a, b, s), r1 = __funnelshift_r(b, c, s);
+    uint32_t t0 = s >= 32 ? r1 : r0;
+    uint32_t t1 = s >= 32 ? __funnelshift_r(c, (uint32_t)(hi >> 32), s) : r1;
+    return (uint64_t)t0 | ((uint64_t)t1 << 32);
 }
 
 template <bool kFloatInput>
 __device__ __forceinline__ void load_point(const uint8_t* rec, Coord c[3], uint32_t col[3]) {
+    uintptr_t addr = reinterpret_cast<uintptr_t>(rec);
+    const uint64_t* q = reinterpret_cast<const uint64_t*>(addr & ~(uintptr_t)7);
+    uint32_t s = (uint32_t)(addr & 7) * 8;
     if (kFloatInput) {
-        c[0] = coord_f32(__uint_as_float(load_u32_unaligned(rec)));
-        c[1] = coord_f32(__uint_as_float(load_u32_unaligned(rec + 4)));
-        c[2] = coord_f32(__uint_as_float(load_u32_unaligned(rec + 8)));
-        col[0] = rec[12];
-        col[1] = rec[13];
-        col[2] = rec[14];
+        uint64_t w0 = q[0], w1 = q[1], w2 = q[2];
+        uint64_t r0 = shr128(w0, w1, s), r1 = shr128(w1, w2, s);
+        c[0] = coord_f32(__uint_as_float((uint32_t)r0));
+        c[1] = coord_f32(__uint_as_float((uint32_t)(r0 >> 32)));
+        c[2] = coord_f32(__uint_as_float((uint32_t)r1));
+        col[0] = (uint32_t)(r1 >> 32) & 0xFF;
+        col[1] = (uint32_t)(r1 >> 40) & 0xFF;
+        col[2] = (uint32_t)(r1 >> 48) & 0xFF;
     } else {
-        c[0] = coord_f64(__longlong_as_double((long long)load_u64_unaligned(rec)));
-        c[1] = coord_f64(__longlong_as_double((long long)load_u64_unaligned(rec + 8)));
-        c[2] = coord_f64(__longlong_as_double((long long)load_u64_unaligned(rec + 16)));
-        col[0] = rec[24];
-        col[1] = rec[25];
-        col[2] = rec[26];
+        uint64_t w0 = q[0], w1 = q[1], w2 = q[2], w3 = q[3], w4 = q[4];
+        uint64_t r0 = shr128(w0, w1, s), r1 = shr128(w1, w2, s), r2 = shr128(w2, w3, s), r3 = shr128(w3, w4, s);
+        c[0] = coord_f64(__longlong_as_double((long long)r0));
+        c[1] = coord_f64(__longlong_as_double((long long)r1));
+        c[2] = coord_f64(__longlong_as_double((long long)r2));
+        col[0] = (uint32_t)r3 & 0xFF;
+        col[1] = (uint32_t)(r3 >> 8) & 0xFF;
+        col[2] = (uint32_t)(r3 >> 16) & 0xFF;
     }
 }
 

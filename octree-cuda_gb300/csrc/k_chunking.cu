@@ -322,16 +322,58 @@ __global__ void __launch_bounds__(kTileThreads) k_distribute(const uint8_t* __re
     }
 }
 
+// Copies byte range [src, src + bytes) to dst.  Both addresses are even (18-byte
+// records); the body is written as aligned 16-byte stores assembled from
+// 4-byte loads, realigned by a 16-bit funnel shift when needed.
+__device__ __forceinline__ void copy_bytes_even(uint8_t* __restrict__ dst, const uint8_t* __restrict__ src,
+                                                uint64_t bytes) {
+    uintptr_t d0 = reinterpret_cast<uintptr_t>(dst), d1 = d0 + bytes;
+    uintptr_t a0 = (d0 + 15) & ~(uintptr_t)15, a1 = d1 & ~(uintptr_t)15;
+    const intptr_t delta = reinterpret_cast<intptr_t>(src) - (intptr_t)d0;
+    if (a0 >= a1) {   // short range: 2-byte copies
+        for (uintptr_t p = d0 + 2 * threadIdx.x; p < d1; p += 2 * blockDim.x)
+            *reinterpret_cast<uint16_t*>(p) = *reinterpret_cast<const uint16_t*>(p + delta);
+        return;
+    }
+    for (uintptr_t p = d0 + 2 * threadIdx.x; p < a0; p += 2 * blockDim.x)
+        *reinterpret_cast<uint16_t*>(p) = *reinterpret_cast<const uint16_t*>(p + delta);
+    for (uintptr_t p = a1 + 2 * threadIdx.x; p < d1; p += 2 * blockDim.x)
+        *reinterpret_cast<uint16_t*>(p) = *reinterpret_cast<const uint16_t*>(p + delta);
+    const uint64_t chunks = (a1 - a0) >> 4;
+    for (uint64_t i = threadIdx.x; i < chunks; i += blockDim.x) {
+        uintptr_t dp = a0 + i * 16, sp = dp + delta;
+        const uint32_t* w = reinterpret_cast<const uint32_t*>(sp & ~(uintptr_t)3);
+        uint4 o;
+        if (sp & 2) {
+            uint32_t w0 = w[0], w1 = w[1], w2 = w[2], w3 = w[3], w4 = w[4];
+            o.x = __funnelshift_r(w0, w1, 16);
+            o.y = __funnelshift_r(w1, w2, 16);
+            o.z = __funnelshift_r(w2, w3, 16);
+            o.w = __funnelshift_r(w3, w4, 16);
+        } else {
+            o.x = w[0];
+            o.y = w[1];
+            o.z = w[2];
+            o.w = w[3];
+        }
+        *reinterpret_cast<uint4*>(dp) = o;
+    }
+}
+
 __global__ void k_place(const uint64_t* __restrict__ src_off, const uint64_t* __restrict__ dst_off,
-                        const uint32_t* __restrict__ count, uint32_t n_nodes, const uint32_t* __restrict__ stage_lut,
-                        const uint8_t* __restrict__ stage_rec, uint32_t* __restrict__ lut, uint8_t* __restrict__ rec) {
+                        const uint32_t* __restrict__ count, uint32_t n_nodes, const uint8_t* __restrict__ stage_rec,
+                        uint8_t* __restrict__ rec) {
+    for (uint32_t v = blockIdx.x; v < n_nodes; v += gridDim.x)
+        copy_bytes_even(rec + dst_off[v] * 18, stage_rec + src_off[v] * 18, (uint64_t)count[v] * 18);
+}
+
+__global__ void k_place_lut(const uint64_t* __restrict__ src_off, const uint64_t* __restrict__ dst_off,
+                            const uint32_t* __restrict__ count, uint32_t n_nodes,
+                            const uint32_t* __restrict__ stage_lut, uint32_t* __restrict__ lut) {
     for (uint32_t v = blockIdx.x; v < n_nodes; v += gridDim.x) {
         uint64_t s = src_off[v], d = dst_off[v];
         uint32_t c = count[v];
         for (uint32_t i = threadIdx.x; i < c; i += blockDim.x) lut[d + i] = stage_lut[s + i];
-        const uint16_t* sr = reinterpret_cast<const uint16_t*>(stage_rec + s * 18);
-        uint16_t* dr = reinterpret_cast<uint16_t*>(rec + d * 18);
-        for (uint64_t i = threadIdx.x; i < (uint64_t)c * 9; i += blockDim.x) dr[i] = sr[i];
     }
 }
 
@@ -420,11 +462,18 @@ int launch_distribute(const uint8_t* cloud, uint64_t n, uint32_t stride, bool fl
 }
 
 int launch_place(const uint64_t* src_off, const uint64_t* dst_off, const uint32_t* count, uint32_t n_nodes,
-                  const uint32_t* stage_lut, const uint8_t* stage_rec, uint32_t* lut, uint8_t* rec,
-                  cudaStream_t stream) {
+                 const uint8_t* stage_rec, uint8_t* rec, cudaStream_t stream) {
     if (!n_nodes) return 0;
-    unsigned grid = n_nodes < 4096 ? n_nodes : 4096;
-    k_place<<<grid, 256, 0, stream>>>(src_off, dst_off, count, n_nodes, stage_lut, stage_rec, lut, rec);
+    unsigned grid = n_nodes < 8192 ? n_nodes : 8192;
+    k_place<<<grid, 256, 0, stream>>>(src_off, dst_off, count, n_nodes, stage_rec, rec);
+    return 1;
+}
+
+int launch_place_lut(const uint64_t* src_off, const uint64_t* dst_off, const uint32_t* count, uint32_t n_nodes,
+                     const uint32_t* stage_lut, uint32_t* lut, cudaStream_t stream) {
+    if (!n_nodes) return 0;
+    unsigned grid = n_nodes < 8192 ? n_nodes : 8192;
+    k_place_lut<<<grid, 256, 0, stream>>>(src_off, dst_off, count, n_nodes, stage_lut, lut);
     return 1;
 }
 

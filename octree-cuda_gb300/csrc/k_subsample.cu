@@ -33,7 +33,10 @@ namespace oc {
 
 namespace {
 
-constexpr int kSubThreads = 1024;
+#ifndef OC_SUB_THREADS
+#define OC_SUB_THREADS 1024
+#endif
+constexpr int kSubThreads = OC_SUB_THREADS;
 constexpr uint32_t kBrickSlots = 8192;    // shared-memory brick table capacity
 constexpr uint32_t kBrickShift = 32 - 13;
 
@@ -132,14 +135,101 @@ struct NodeShared {
     uint32_t cells;
 };
 
-// Candidate j of the current node: which child, and its position there.
-__device__ __forceinline__ void locate(const NodeShared& ns, uint32_t j, uint32_t& c, uint64_t& pos) {
-    c = 0;
-    while (c + 1 < ns.nchild && ns.prefix[c + 1] <= j) ++c;
-    pos = ns.start[c] + (j - ns.prefix[c]);
+__device__ __forceinline__ uint32_t nth_set_bit(uint64_t m, uint32_t n) {
+    uint32_t lo = (uint32_t)m, hi = (uint32_t)(m >> 32);
+    uint32_t pl = (uint32_t)__popc(lo);
+    return n < pl ? (uint32_t)__fns(lo, 0, (int)n + 1) : 32u + (uint32_t)__fns(hi, 0, (int)(n - pl) + 1);
 }
 
-template <bool kF32>
+// Visits every occupied cell of the 3x3x3 neighbourhood of the cell at
+// brick-local (lx, ly, lz) of brick (bx, by, bz) held in `slot` (the cell
+// itself included), calling f(rank, x, y, z) with grid coordinates.
+// Only the bricks across the faces that the cell touches are looked up; each
+// of the nine x-rows of the neighbourhood is read as a 4-bit slice of a brick
+// mask, so ranks are computed for occupied neighbours only.
+template <class F>
+__device__ __forceinline__ void visit_neighbours(const BrickMap& bm, uint32_t slot, int bx, int by, int bz, int lx,
+                                                 int ly, int lz, F& f) {
+    const int sx = lx == 0 ? -1 : (lx == 3 ? 1 : 0);
+    const int sy = ly == 0 ? -1 : (ly == 3 ? 1 : 0);
+    const int sz = lz == 0 ? -1 : (lz == 3 ? 1 : 0);
+    auto find = [&](int dx, int dy, int dz) -> int {
+        const int nx = bx + dx, ny = by + dy, nz = bz + dz;
+        if (nx < 0 || ny < 0 || nz < 0 || nx >= (int)bm.bs || ny >= (int)bm.bs || nz >= (int)bm.bs) return -1;
+        return brick_find(bm, (uint32_t)(nx + bm.bs * (ny + bm.bs * nz)) + 1);
+    };
+    // slots of the (up to) eight bricks: index bit 0 = x side, 1 = y side, 2 = z side
+    const int s0 = (int)slot;
+    const int s1 = sx ? find(sx, 0, 0) : -1;
+    const int s2 = sy ? find(0, sy, 0) : -1;
+    const int s3 = (sx && sy) ? find(sx, sy, 0) : -1;
+    const int s4 = sz ? find(0, 0, sz) : -1;
+    const int s5 = (sx && sz) ? find(sx, 0, sz) : -1;
+    const int s6 = (sy && sz) ? find(0, sy, sz) : -1;
+    const int s7 = (sx && sy && sz) ? find(sx, sy, sz) : -1;
+    // x window inside the cell's own brick column, and the side brick's edge column
+    const uint32_t xlo = (uint32_t)max(lx - 1, 0), xhi = (uint32_t)min(lx + 1, 3);
+    const uint32_t own_x = ((2u << xhi) - 1u) & ~((1u << xlo) - 1u);
+    const uint32_t side_bit = sx < 0 ? 3u : 0u;
+#pragma unroll
+    for (int dz = -1; dz <= 1; ++dz) {
+#pragma unroll
+        for (int dy = -1; dy <= 1; ++dy) {
+            const int yy = ly + dy, zz = lz + dz;
+            const bool ys = yy < 0 || yy > 3, zs = zz < 0 || zz > 3;
+            if ((ys && sy != (dy < 0 ? -1 : 1)) || (zs && sz != (dz < 0 ? -1 : 1))) continue;
+            const uint32_t row = (uint32_t)((yy & 3) * 4 + (zz & 3) * 16);
+            const int so = zs ? (ys ? s6 : s4) : (ys ? s2 : s0);
+            const int ss = zs ? (ys ? s7 : s5) : (ys ? s3 : s1);
+            if (so >= 0) {
+                const uint64_t m = bm.mask[so];
+                uint32_t sel = (uint32_t)(m >> row) & own_x;
+                const uint32_t base = bm.base[so];
+                while (sel) {
+                    const uint32_t x = (uint32_t)__ffs(sel) - 1;
+                    sel &= sel - 1;
+                    const uint32_t bit = row + x;
+                    f(base + (uint32_t)__popcll(m & ((1ull << bit) - 1ull)), bx * 4 + (int)x, by * 4 + yy, bz * 4 + zz);
+                }
+            }
+            if (sx && ss >= 0) {
+                const uint64_t m = bm.mask[ss];
+                const uint32_t bit = row + side_bit;
+                if ((m >> bit) & 1ull)
+                    f(bm.base[ss] + (uint32_t)__popcll(m & ((1ull << bit) - 1ull)), (bx + sx) * 4 + (int)side_bit,
+                      by * 4 + yy, bz * 4 + zz);
+            }
+        }
+    }
+}
+
+struct InterSum {
+    const uint64_t* acc;
+    uint64_t e;
+    __device__ __forceinline__ void operator()(uint32_t n, int, int, int) { e += acc[n]; }
+};
+
+struct WeightedSum {
+    const uint32_t* start;
+    const uint32_t* count;
+    const uint8_t* pts;
+    int x, y, z;
+    uint64_t sr, sg, sb, sw;
+    __device__ __forceinline__ void operator()(uint32_t n, int, int, int) {
+        const uint32_t s0 = start[n], s1 = s0 + count[n];
+        for (uint32_t p = s0; p < s1; ++p) {
+            const uint32_t* q = reinterpret_cast<const uint32_t*>(pts + (uint64_t)p * 20);
+            const uint32_t wq = weight_q(__uint_as_float(q[0]), __uint_as_float(q[1]), __uint_as_float(q[2]), x, y, z);
+            sr += (uint64_t)wq * (q[3] & 0xFFFF);
+            sg += (uint64_t)wq * (q[3] >> 16);
+            sb += (uint64_t)wq * (q[4] & 0xFFFF);
+            sw += wq;
+        }
+    }
+};
+
+// kColor: 0 raw colour, 1 intra-cell, 2 inter-cell, 3 distance-weighted inter-cell
+template <bool kF32, int kColor, bool kRandom>
 __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
     extern __shared__ uint64_t dyn[];
     __shared__ NodeShared ns;
@@ -161,11 +251,11 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
     gl_map.key = a.global_key + (uint64_t)blockIdx.x * a.global_cap;
     gl_map.base = a.global_base + (uint64_t)blockIdx.x * a.global_cap;
 
-    const bool intra = (a.mode & kModeIntra) != 0;
-    const bool inter = !intra && (a.mode & kModeInter) != 0;
-    const bool weighted = inter && (a.mode & kModeWeight) != 0;
-    const bool random = (a.mode & kModeRandom) != 0;
-    const bool averaged = intra || inter;
+    constexpr bool intra = kColor == 1;
+    constexpr bool inter = kColor >= 2;
+    constexpr bool weighted = kColor == 3;
+    constexpr bool random = kRandom;
+    constexpr bool averaged = intra || inter;
 
     for (;;) {
         if (threadIdx.x == 0) ns.node = atomicAdd(a.work_counter, 1u);
@@ -186,8 +276,9 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
             ns.prefix[nd.nchild] = p;
         }
         const AxisGrid ax0 = nd.ax[0], ax1 = nd.ax[1], ax2 = nd.ax[2];
-        const uint32_t p_in = nd.p_in;
         const uint64_t off = nd.cand_off;
+        const uint32_t level = nd.level;
+        const uint64_t morton = nd.morton;
         BrickMap bm = sm_map;
 
         // ---- pass A: cells and occupancy.  A node whose bricks exceed 70% of
@@ -203,41 +294,44 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
             }
             __syncthreads();
             const uint32_t limit = bm.cap - (bm.cap >> 2) - (bm.cap >> 4);
-            for (uint32_t j = threadIdx.x; j < p_in; j += blockDim.x) {
-                if (*(volatile uint32_t*)&s_overflow) break;
-                uint32_t c;
-                uint64_t pos;
-                locate(ns, j, c, pos);
-                bool staged = (ns.kind >> c) & 1u;
-                uint32_t idx = staged ? a.stage_lut[pos] : a.leaf_lut[pos];
-                Coord co[3];
-                uint32_t col[3];
-                load_point<kF32>(a.cloud + (uint64_t)idx * a.stride, co, col);
-                float ux, uy, uz;
-                int ix = axis_cell<kF32>(co[0], ax0, a.grid, ux);
-                int iy = axis_cell<kF32>(co[1], ax1, a.grid, uy);
-                int iz = axis_cell<kF32>(co[2], ax2, a.grid, uz);
-                if ((ix | iy | iz) < 0) {
-                    atomicOr(a.err, kErrBelowBox);
-                    ix = max(ix, 0);
-                    iy = max(iy, 0);
-                    iz = max(iz, 0);
-                }
-                uint32_t b = ((uint32_t)ix >> 2) + bm.bs * (((uint32_t)iy >> 2) + bm.bs * ((uint32_t)iz >> 2));
-                uint32_t bit = (ix & 3) | ((iy & 3) << 2) | ((iz & 3) << 4);
-                bool fresh;
-                uint32_t slot = brick_insert(bm, b + 1, fresh);
-                if (fresh && atomicAdd(&s_bricks, 1u) + 1 >= limit) s_overflow = 1;
-                if (slot >= bm.cap) {
-                    s_overflow = 1;
-                    break;
-                }
-                atomicOr(reinterpret_cast<unsigned long long*>(&bm.mask[slot]), 1ull << bit);
-                a.key_cache[off + j] = (slot << 6) | bit;
-                if (weighted) {
-                    a.unit_cache[(off + j) * 3 + 0] = ux;
-                    a.unit_cache[(off + j) * 3 + 1] = uy;
-                    a.unit_cache[(off + j) * 3 + 2] = uz;
+            for (uint32_t c = 0; c < ns.nchild; ++c) {
+                const uint32_t cnt = ns.count[c];
+                const uint64_t start = ns.start[c];
+                const uint32_t jbase = ns.prefix[c];
+                const uint32_t* src_lut = ((ns.kind >> c) & 1u) ? a.stage_lut : a.leaf_lut;
+                for (uint32_t k = threadIdx.x; k < cnt; k += blockDim.x) {
+                    if (*(volatile uint32_t*)&s_overflow) break;
+                    const uint32_t j = jbase + k;
+                    const uint32_t idx = src_lut[start + k];
+                    Coord co[3];
+                    uint32_t col[3];
+                    load_point<kF32>(a.cloud + (uint64_t)idx * a.stride, co, col);
+                    float ux, uy, uz;
+                    int ix = axis_cell<kF32>(co[0], ax0, a.grid, ux);
+                    int iy = axis_cell<kF32>(co[1], ax1, a.grid, uy);
+                    int iz = axis_cell<kF32>(co[2], ax2, a.grid, uz);
+                    if ((ix | iy | iz) < 0) {
+                        atomicOr(a.err, kErrBelowBox);
+                        ix = max(ix, 0);
+                        iy = max(iy, 0);
+                        iz = max(iz, 0);
+                    }
+                    uint32_t b = ((uint32_t)ix >> 2) + bm.bs * (((uint32_t)iy >> 2) + bm.bs * ((uint32_t)iz >> 2));
+                    uint32_t bit = (ix & 3) | ((iy & 3) << 2) | ((iz & 3) << 4);
+                    bool fresh;
+                    uint32_t slot = brick_insert(bm, b + 1, fresh);
+                    if (fresh && atomicAdd(&s_bricks, 1u) + 1 >= limit) s_overflow = 1;
+                    if (slot >= bm.cap) {
+                        s_overflow = 1;
+                        break;
+                    }
+                    atomicOr(reinterpret_cast<unsigned long long*>(&bm.mask[slot]), 1ull << bit);
+                    a.key_cache[off + j] = (slot << 6) | bit;
+                    if (weighted) {
+                        a.unit_cache[(off + j) * 3 + 0] = ux;
+                        a.unit_cache[(off + j) * 3 + 1] = uy;
+                        a.unit_cache[(off + j) * 3 + 2] = uz;
+                    }
                 }
             }
             __syncthreads();
@@ -258,15 +352,16 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
 
         // ---- ranks of occupied cells (each thread scans a run of slots)
         {
-            const uint32_t per = bm.cap / blockDim.x;
+            const uint32_t per = (bm.cap + blockDim.x - 1) / blockDim.x;
             const uint32_t first = threadIdx.x * per;
+            const uint32_t last = min(first + per, bm.cap);
             uint32_t sum = 0;
-            for (uint32_t k = 0; k < per; ++k) sum += (uint32_t)__popcll(bm.mask[first + k]);
+            for (uint32_t k = first; k < last; ++k) sum += (uint32_t)__popcll(bm.mask[k]);
             uint32_t total;
             uint32_t pre = block_exclusive_scan(sum, warp_sums, total);
-            for (uint32_t k = 0; k < per; ++k) {
-                bm.base[first + k] = pre;
-                pre += (uint32_t)__popcll(bm.mask[first + k]);
+            for (uint32_t k = first; k < last; ++k) {
+                bm.base[k] = pre;
+                pre += (uint32_t)__popcll(bm.mask[k]);
             }
             if (threadIdx.x == 0) ns.cells = total;
         }
@@ -280,25 +375,28 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
         __syncthreads();
 
         // ---- pass B: selection and colour sums
-        for (uint32_t j = threadIdx.x; j < p_in; j += blockDim.x) {
-            uint32_t kc = a.key_cache[off + j];
-            uint32_t slot = kc >> 6, bit = kc & 63;
-            if (slot >= bm.cap) continue;
-            uint32_t rank = bm.base[slot] + (uint32_t)__popcll(bm.mask[slot] & ((1ull << bit) - 1ull));
-            uint32_t c;
-            uint64_t pos;
-            locate(ns, j, c, pos);
-            bool staged = (ns.kind >> c) & 1u;
-            uint32_t idx = staged ? a.stage_lut[pos] : a.leaf_lut[pos];
-            uint64_t key = idx;
-            if (random) key |= (uint64_t)rp_priority(a.seed, nd.level, nd.morton, idx) << 32;
-            atomicMin(reinterpret_cast<unsigned long long*>(&a.acc_best[off + rank]), (unsigned long long)key);
-            if (averaged && !weighted) {
-                const uint16_t* src = reinterpret_cast<const uint16_t*>((staged ? a.stage_rec : a.leaf_rec) + pos * 18);
-                uint64_t enc = encode_colors(src[6], src[7], src[8]);
-                atomicAdd(reinterpret_cast<unsigned long long*>(&a.acc_intra[off + rank]), (unsigned long long)enc);
+        for (uint32_t c = 0; c < ns.nchild; ++c) {
+            const uint32_t cnt = ns.count[c];
+            const uint64_t start = ns.start[c];
+            const uint32_t jbase = ns.prefix[c];
+            const bool staged = (ns.kind >> c) & 1u;
+            const uint32_t* src_lut = staged ? a.stage_lut : a.leaf_lut;
+            const uint8_t* src_rec = staged ? a.stage_rec : a.leaf_rec;
+            for (uint32_t k = threadIdx.x; k < cnt; k += blockDim.x) {
+                uint32_t kc = a.key_cache[off + jbase + k];
+                uint32_t slot = kc >> 6, bit = kc & 63;
+                uint32_t rank = bm.base[slot] + (uint32_t)__popcll(bm.mask[slot] & ((1ull << bit) - 1ull));
+                uint32_t idx = src_lut[start + k];
+                uint64_t key = idx;
+                if constexpr (random) key |= (uint64_t)rp_priority(a.seed, level, morton, idx) << 32;
+                atomicMin(reinterpret_cast<unsigned long long*>(&a.acc_best[off + rank]), (unsigned long long)key);
+                if (averaged && !weighted) {
+                    const uint16_t* src = reinterpret_cast<const uint16_t*>(src_rec + (start + k) * 18);
+                    uint64_t enc = encode_colors(src[6], src[7], src[8]);
+                    atomicAdd(reinterpret_cast<unsigned long long*>(&a.acc_intra[off + rank]), (unsigned long long)enc);
+                }
+                if (weighted) atomicAdd(&a.csr_count[off + rank], 1u);
             }
-            if (weighted) atomicAdd(&a.csr_count[off + rank], 1u);
         }
         __syncthreads();
 
@@ -317,57 +415,52 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
                 running += total;
             }
             __syncthreads();
-            for (uint32_t j = threadIdx.x; j < p_in; j += blockDim.x) {
-                uint32_t kc = a.key_cache[off + j];
-                uint32_t slot = kc >> 6, bit = kc & 63;
-                if (slot >= bm.cap) continue;
-                uint32_t rank = bm.base[slot] + (uint32_t)__popcll(bm.mask[slot] & ((1ull << bit) - 1ull));
-                uint32_t p = a.csr_start[off + rank] + atomicAdd(&a.csr_count[off + rank], 1u);
-                uint32_t c;
-                uint64_t pos;
-                locate(ns, j, c, pos);
-                bool staged = (ns.kind >> c) & 1u;
-                const uint16_t* src = reinterpret_cast<const uint16_t*>((staged ? a.stage_rec : a.leaf_rec) + pos * 18);
-                uint32_t* dst = reinterpret_cast<uint32_t*>(a.csr_pts + (off + p) * 20);
-                dst[0] = __float_as_uint(a.unit_cache[(off + j) * 3 + 0]);
-                dst[1] = __float_as_uint(a.unit_cache[(off + j) * 3 + 1]);
-                dst[2] = __float_as_uint(a.unit_cache[(off + j) * 3 + 2]);
-                dst[3] = (uint32_t)src[6] | ((uint32_t)src[7] << 16);
-                dst[4] = (uint32_t)src[8];
+            for (uint32_t c = 0; c < ns.nchild; ++c) {
+                const uint32_t cnt = ns.count[c];
+                const uint64_t start = ns.start[c];
+                const uint32_t jbase = ns.prefix[c];
+                const uint8_t* src_rec = ((ns.kind >> c) & 1u) ? a.stage_rec : a.leaf_rec;
+                for (uint32_t k = threadIdx.x; k < cnt; k += blockDim.x) {
+                    const uint32_t j = jbase + k;
+                    uint32_t kc = a.key_cache[off + j];
+                    uint32_t slot = kc >> 6, bit = kc & 63;
+                    uint32_t rank = bm.base[slot] + (uint32_t)__popcll(bm.mask[slot] & ((1ull << bit) - 1ull));
+                    uint32_t p = a.csr_start[off + rank] + atomicAdd(&a.csr_count[off + rank], 1u);
+                    const uint16_t* src = reinterpret_cast<const uint16_t*>(src_rec + (start + k) * 18);
+                    uint32_t* dst = reinterpret_cast<uint32_t*>(a.csr_pts + (off + p) * 20);
+                    dst[0] = __float_as_uint(a.unit_cache[(off + j) * 3 + 0]);
+                    dst[1] = __float_as_uint(a.unit_cache[(off + j) * 3 + 1]);
+                    dst[2] = __float_as_uint(a.unit_cache[(off + j) * 3 + 2]);
+                    dst[3] = (uint32_t)src[6] | ((uint32_t)src[7] << 16);
+                    dst[4] = (uint32_t)src[8];
+                }
             }
             __syncthreads();
         }
 
-        // ---- emit one record per occupied cell
+        // ---- emit one record per occupied cell (thread per cell, rank order)
         for (uint32_t r = threadIdx.x; r < cells; r += blockDim.x) {
-            // slot holding rank r: last slot with base <= r and a non-empty mask
+            // slot holding rank r: the last slot whose base is <= r (bases are
+            // non-decreasing; the next non-empty slot starts above r)
             uint32_t lo = 0, hi = bm.cap - 1;
             while (lo < hi) {
                 uint32_t mid = (lo + hi + 1) >> 1;
                 if (bm.base[mid] <= r) lo = mid;
                 else hi = mid - 1;
             }
-            uint32_t slot = lo;
-            while (slot > 0 && (bm.mask[slot] == 0 || bm.base[slot] > r)) --slot;
-            uint64_t mk = bm.mask[slot];
-            uint32_t want = r - bm.base[slot];
-            uint32_t bit = 0;
-            for (uint32_t seen = 0; bit < 64; ++bit) {
-                if ((mk >> bit) & 1ull) {
-                    if (seen == want) break;
-                    ++seen;
-                }
-            }
-            if (bit >= 64) {
+            const uint32_t slot = lo;
+            const uint64_t mk = bm.mask[slot];
+            const uint32_t want = r - bm.base[slot];
+            if (want >= (uint32_t)__popcll(mk)) {
                 atomicOr(a.err, kErrProbe);
-                bit = 0;
+                continue;
             }
-            uint32_t brick = bm.key[slot] - 1;
-            int bx = (int)(brick % bm.bs), by = (int)((brick / bm.bs) % bm.bs), bz = (int)(brick / (bm.bs * bm.bs));
-            int x = bx * 4 + (int)(bit & 3), y = by * 4 + (int)((bit >> 2) & 3), z = bz * 4 + (int)((bit >> 4) & 3);
-
-            uint64_t best = a.acc_best[off + r];
-            uint32_t idx = (uint32_t)best;
+            const uint32_t bit = nth_set_bit(mk, want);
+            const uint32_t brick = bm.key[slot] - 1;
+            const int bx = (int)(brick % bm.bs), by = (int)((brick / bm.bs) % bm.bs), bz = (int)(brick / (bm.bs * bm.bs));
+            const int lx = (int)(bit & 3), ly = (int)((bit >> 2) & 3), lz = (int)((bit >> 4) & 3);
+            const uint64_t best = a.acc_best[off + r];
+            const uint32_t idx = (uint32_t)best;
             Coord co[3];
             uint32_t col[3];
             load_point<kF32>(a.cloud + (uint64_t)idx * a.stride, co, col);
@@ -375,36 +468,17 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
             if (intra) {
                 decode_colors(a.acc_intra[off + r], cr, cg, cb);
             } else if (inter && !weighted) {
-                uint64_t e = 0;
-                for (int ox = -1; ox <= 1; ++ox)
-                    for (int oy = -1; oy <= 1; ++oy)
-                        for (int oz = -1; oz <= 1; ++oz) {
-                            int n = cell_rank(bm, x + ox, y + oy, z + oz);
-                            if (n >= 0) e += a.acc_intra[off + n];
-                        }
-                decode_colors(e, cr, cg, cb);
+                InterSum f{a.acc_intra + off, 0};
+                visit_neighbours(bm, slot, bx, by, bz, lx, ly, lz, f);
+                decode_colors(f.e, cr, cg, cb);
             } else if (weighted) {
-                uint64_t sr = 0, sg = 0, sb = 0, sw = 0;
-                for (int ox = -1; ox <= 1; ++ox)
-                    for (int oy = -1; oy <= 1; ++oy)
-                        for (int oz = -1; oz <= 1; ++oz) {
-                            int n = cell_rank(bm, x + ox, y + oy, z + oz);
-                            if (n < 0) continue;
-                            uint32_t s0 = a.csr_start[off + n], s1 = s0 + a.csr_count[off + n];
-                            for (uint32_t p = s0; p < s1; ++p) {
-                                const uint32_t* q = reinterpret_cast<const uint32_t*>(a.csr_pts + (off + p) * 20);
-                                uint32_t wq = weight_q(__uint_as_float(q[0]), __uint_as_float(q[1]),
-                                                       __uint_as_float(q[2]), x, y, z);
-                                sr += (uint64_t)wq * (q[3] & 0xFFFF);
-                                sg += (uint64_t)wq * (q[3] >> 16);
-                                sb += (uint64_t)wq * (q[4] & 0xFFFF);
-                                sw += wq;
-                            }
-                        }
-                if (sw) {
-                    cr = (uint16_t)(sr / sw);
-                    cg = (uint16_t)(sg / sw);
-                    cb = (uint16_t)(sb / sw);
+                WeightedSum f{a.csr_start + off, a.csr_count + off, a.csr_pts + off * 20,
+                              bx * 4 + lx, by * 4 + ly, bz * 4 + lz, 0, 0, 0, 0};
+                visit_neighbours(bm, slot, bx, by, bz, lx, ly, lz, f);
+                if (f.sw) {
+                    cr = (uint16_t)(f.sr / f.sw);
+                    cg = (uint16_t)(f.sg / f.sw);
+                    cb = (uint16_t)(f.sb / f.sw);
                 }
             }
             int32_t ox_ = out_coord<kF32>(co[0], a.out.ax[0]);
@@ -429,17 +503,41 @@ size_t subsample_smem_bytes() {
     return (size_t)kBrickSlots * (8 + 4 + 4);
 }
 
+namespace {
+
+template <bool kF32, int kColor, bool kRandom>
+void launch_one(const SubLevelArgs& a, int grid, size_t smem, cudaStream_t stream) {
+    cudaFuncSetAttribute(k_subsample<kF32, kColor, kRandom>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_subsample<kF32, kColor, kRandom><<<grid, kSubThreads, smem, stream>>>(a);
+}
+
+template <bool kF32>
+void launch_mode(const SubLevelArgs& a, int grid, size_t smem, cudaStream_t stream) {
+    const bool intra = (a.mode & kModeIntra) != 0;
+    const bool inter = !intra && (a.mode & kModeInter) != 0;
+    const bool weighted = inter && (a.mode & kModeWeight) != 0;
+    const int color = intra ? 1 : (weighted ? 3 : (inter ? 2 : 0));
+    const bool random = (a.mode & kModeRandom) != 0;
+    switch (color * 2 + (random ? 1 : 0)) {
+    case 0: launch_one<kF32, 0, false>(a, grid, smem, stream); break;
+    case 1: launch_one<kF32, 0, true>(a, grid, smem, stream); break;
+    case 2: launch_one<kF32, 1, false>(a, grid, smem, stream); break;
+    case 3: launch_one<kF32, 1, true>(a, grid, smem, stream); break;
+    case 4: launch_one<kF32, 2, false>(a, grid, smem, stream); break;
+    case 5: launch_one<kF32, 2, true>(a, grid, smem, stream); break;
+    case 6: launch_one<kF32, 3, false>(a, grid, smem, stream); break;
+    default: launch_one<kF32, 3, true>(a, grid, smem, stream); break;
+    }
+}
+
+}   // namespace
+
 int launch_subsample_level(const SubLevelArgs& a, int num_sms, cudaStream_t stream) {
     if (!a.n_nodes) return 0;
     size_t smem = subsample_smem_bytes();
     int grid = (int)std::min<uint32_t>(a.n_nodes, (uint32_t)num_sms);
-    if (a.float_input) {
-        cudaFuncSetAttribute(k_subsample<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_subsample<true><<<grid, kSubThreads, smem, stream>>>(a);
-    } else {
-        cudaFuncSetAttribute(k_subsample<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_subsample<false><<<grid, kSubThreads, smem, stream>>>(a);
-    }
+    if (a.float_input) launch_mode<true>(a, grid, smem, stream);
+    else launch_mode<false>(a, grid, smem, stream);
     return 1;
 }
 

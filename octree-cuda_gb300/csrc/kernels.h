@@ -104,9 +104,11 @@ size_t subsample_smem_bytes();
 uint32_t subsample_block_size();
 int launch_subsample_level(const SubLevelArgs& a, int num_sms, cudaStream_t stream);
 
-// Moves staged internal-node outputs to their final (post-order) positions.
+// Moves staged internal-node records to their final (post-order) positions.
 int launch_place(const uint64_t* src_off, const uint64_t* dst_off, const uint32_t* count, uint32_t n_nodes,
-                  const uint32_t* stage_lut, const uint8_t* stage_rec, uint32_t* lut, uint8_t* rec,
-                  cudaStream_t stream);
+                 const uint8_t* stage_rec, uint8_t* rec, cudaStream_t stream);
+// Same for the per-record cloud indices.
+int launch_place_lut(const uint64_t* src_off, const uint64_t* dst_off, const uint32_t* count, uint32_t n_nodes,
+                     const uint32_t* stage_lut, uint32_t* lut, cudaStream_t stream);
 
 }   // namespace oc
