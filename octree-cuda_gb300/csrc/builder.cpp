@@ -310,8 +310,22 @@ void Builder::subsample() {
     for (int a = 0; a < 3; ++a) op.ax[a] = make_out_axis(cfg_.bb_min[a], 1.0 / cfg_.scale[a]);
 
     for (uint32_t l = 1; l <= depth_; ++l) {
-        const auto& list = internal_by_level_[l];
+        auto& list = internal_by_level_[l];
         if (list.empty()) continue;
+        // largest nodes first: the persistent blocks take them in this order
+        auto p_in_of = [&](uint32_t vi) {
+            const NodeHost& v = nodes_[vi];
+            uint64_t p = 0;
+            uint32_t c = v.child_first;
+            for (uint32_t s = 0; s < 8; ++s)
+                if (v.mask & (1u << s)) p += nodes_[c++].points;
+            return p;
+        };
+        std::vector<std::pair<uint64_t, uint32_t>> order;
+        for (uint32_t vi : list) order.push_back({p_in_of(vi), vi});
+        std::stable_sort(order.begin(), order.end(),
+                         [](const auto& x, const auto& y) { return x.first > y.first; });
+        for (size_t k = 0; k < list.size(); ++k) list[k] = order[k].second;
         const double side = cubic / std::pow(2.0, (double)(depth_ - l));   // fp_subsampling.cu:16-17
         const double t = side / S;                                         // kernel_helpers.cuh:14
         std::vector<SubNode> table(list.size());
@@ -320,7 +334,10 @@ void Builder::subsample() {
             const NodeHost& v = nodes_[list[k]];
             SubNode& sn = table[k];
             std::memset(&sn, 0, sizeof(sn));
-            for (int a = 0; a < 3; ++a) sn.ax[a] = make_axis(v.mn[a], t);
+            for (int a = 0; a < 3; ++a) {
+                sn.ax[a] = make_axis(v.mn[a], t);
+                sn.qa[a] = make_qaxis(v.mn[a], cfg_.bb_min[a], 1.0 / cfg_.scale[a], t);
+            }
             sn.morton = v.key;
             sn.level = l;
             uint32_t c = v.child_first, nc = 0;
@@ -349,6 +366,8 @@ void Builder::subsample() {
         // scratch and staging capacity
         key_cache_.ensure(level_in * 4);
         acc_best_.ensure(level_in * 8);
+        cell_slot_.ensure(level_in * 4);
+        if (cfg_.random) acc_sel_.ensure(level_in * 4);
         if (averaged && !weighted) acc_intra_.ensure(level_in * 8);
         if (weighted) {
             unit_cache_.ensure(level_in * 12);
@@ -383,6 +402,8 @@ void Builder::subsample() {
         a.key_cache = key_cache_.as<uint32_t>();
         a.unit_cache = unit_cache_.as<float>();
         a.acc_best = acc_best_.as<uint64_t>();
+        a.acc_sel = acc_sel_.as<uint32_t>();
+        a.cell_slot = cell_slot_.as<uint32_t>();
         a.acc_intra = acc_intra_.as<uint64_t>();
         a.csr_count = csr_count_.as<uint32_t>();
         a.csr_start = csr_start_.as<uint32_t>();

@@ -265,15 +265,28 @@ __device__ __forceinline__ uint64_t encode_colors(uint32_t r, uint32_t g, uint32
 }
 
 __device__ __forceinline__ void decode_colors(uint64_t e, uint16_t& r, uint16_t& g, uint16_t& b) {
-    uint32_t amount = (uint32_t)(e & 0x3FF);
+    const uint32_t amount = (uint32_t)(e & 0x3FF);
     if (amount == 0) {
         r = g = b = 0xFFFF;
         return;
     }
-    r = (uint16_t)((uint32_t)((e >> 46) & 0xFFFF) / amount);
-    g = (uint16_t)((uint32_t)((e >> 28) & 0xFFFF) / amount);
-    b = (uint16_t)((uint32_t)((e >> 10) & 0xFFFF) / amount);
+    const uint32_t xr = (uint32_t)((e >> 46) & 0xFFFF), xg = (uint32_t)((e >> 28) & 0xFFFF),
+                   xb = (uint32_t)((e >> 10) & 0xFFFF);
+    if (amount == 1) {
+        r = (uint16_t)xr;
+        g = (uint16_t)xg;
+        b = (uint16_t)xb;
+        return;
+    }
+    // floor(x / d) = umulhi(x, ceil(2^32 / d)) exactly for x < 2^16, d < 2^10:
+    // the product overshoots x / d by less than 2^-16, below the 1/d gap to
+    // the next integer
+    const uint32_t m = 0xFFFFFFFFu / amount + 1u;
+    r = (uint16_t)__umulhi(xr, m);
+    g = (uint16_t)__umulhi(xg, m);
+    b = (uint16_t)__umulhi(xb, m);
 }
+
 
 // ---------------------------------------------------------------------------
 // Distance weighting.  exp(x) for x in [-15, 0] by Cody & Waite range

@@ -46,7 +46,7 @@ struct BrickMap {
     uint32_t* base;   // rank of the brick's first cell
     uint32_t cap;     // slots (power of two, multiple of the block size)
     uint32_t shift;   // 32 - log2(cap)
-    uint32_t bs;      // bricks per axis
+    uint32_t bs;      // bricks per axis (<= 256): brick id = bx | by << 8 | bz << 16
     uint32_t grid;    // S
 };
 
@@ -87,18 +87,6 @@ __device__ __forceinline__ int brick_find(const BrickMap& m, uint32_t b1) {
     return -1;
 }
 
-// Rank of cell (x, y, z) or -1 when unoccupied / outside the grid.
-__device__ __forceinline__ int cell_rank(const BrickMap& m, int x, int y, int z) {
-    if (x < 0 || y < 0 || z < 0 || x >= (int)m.grid || y >= (int)m.grid || z >= (int)m.grid) return -1;
-    uint32_t b = ((uint32_t)x >> 2) + m.bs * (((uint32_t)y >> 2) + m.bs * ((uint32_t)z >> 2));
-    int s = brick_find(m, b + 1);
-    if (s < 0) return -1;
-    uint32_t bit = (x & 3) | ((y & 3) << 2) | ((z & 3) << 4);
-    uint64_t mk = m.mask[s];
-    if (!((mk >> bit) & 1ull)) return -1;
-    return (int)(m.base[s] + __popcll(mk & ((1ull << bit) - 1ull)));
-}
-
 __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* warp_sums, uint32_t& total) {
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint32_t x = v;
@@ -125,6 +113,32 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* w
     return warp_prefix + x - v;
 }
 
+// Cell index of one axis from the candidate's quantised coordinate q, or -2
+// when the interval of positions q stands for straddles a cell boundary (the
+// binary64 path then decides).  The interval [lo - e, lo + B + e] holds the
+// reference's cell-unit value: e bounds the fp32 rounding of lo and of the
+// host-rounded constants (a few ulp of |lo| + |base| + B) with a wide margin.
+__device__ __forceinline__ int quant_cell(int32_t q, const QAxis& a, uint32_t G) {
+    const int32_t dq = q - a.qn;
+    if (dq > (1 << 22) || dq < -(1 << 22)) return -2;
+    const float lo = __fmaf_rn((float)dq, a.B, a.base);
+    const float e =
+        __fmul_rn(__fadd_rn(__fadd_rn(fabsf(lo), fabsf(a.base)), __fadd_rn(a.B, 4.0f)), 9.5367431640625e-07f);
+    const int i0 = idx_from_units(__fsub_rn(lo, e), G);
+    const int i1 = idx_from_units(__fadd_rn(__fadd_rn(lo, a.B), e), G);
+    return (i0 == i1 && i0 >= 0) ? i0 : -2;
+}
+
+// Cell-unit position used by distance weighting: the centre of the candidate's
+// quantisation step, ((q - qn) + 1/2) * B + base, in fp32.
+__device__ __forceinline__ float quant_units(int32_t q, const QAxis& a) {
+    return __fmaf_rn(__fadd_rn((float)(q - a.qn), 0.5f), a.B, a.base);
+}
+
+__device__ __forceinline__ int32_t rec_coord(const uint16_t* r, int i) {
+    return (int32_t)((uint32_t)r[2 * i] | ((uint32_t)r[2 * i + 1] << 16));
+}
+
 struct NodeShared {
     uint64_t start[8];
     uint32_t count[8];
@@ -134,12 +148,6 @@ struct NodeShared {
     uint32_t node;
     uint32_t cells;
 };
-
-__device__ __forceinline__ uint32_t nth_set_bit(uint64_t m, uint32_t n) {
-    uint32_t lo = (uint32_t)m, hi = (uint32_t)(m >> 32);
-    uint32_t pl = (uint32_t)__popc(lo);
-    return n < pl ? (uint32_t)__fns(lo, 0, (int)n + 1) : 32u + (uint32_t)__fns(hi, 0, (int)(n - pl) + 1);
-}
 
 // Visits every occupied cell of the 3x3x3 neighbourhood of the cell at
 // brick-local (lx, ly, lz) of brick (bx, by, bz) held in `slot` (the cell
@@ -156,7 +164,7 @@ __device__ __forceinline__ void visit_neighbours(const BrickMap& bm, uint32_t sl
     auto find = [&](int dx, int dy, int dz) -> int {
         const int nx = bx + dx, ny = by + dy, nz = bz + dz;
         if (nx < 0 || ny < 0 || nz < 0 || nx >= (int)bm.bs || ny >= (int)bm.bs || nz >= (int)bm.bs) return -1;
-        return brick_find(bm, (uint32_t)(nx + bm.bs * (ny + bm.bs * nz)) + 1);
+        return brick_find(bm, ((uint32_t)nx | ((uint32_t)ny << 8) | ((uint32_t)nz << 16)) + 1);
     };
     // slots of the (up to) eight bricks: index bit 0 = x side, 1 = y side, 2 = z side
     const int s0 = (int)slot;
@@ -276,6 +284,7 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
             ns.prefix[nd.nchild] = p;
         }
         const AxisGrid ax0 = nd.ax[0], ax1 = nd.ax[1], ax2 = nd.ax[2];
+        const QAxis qa0 = nd.qa[0], qa1 = nd.qa[1], qa2 = nd.qa[2];
         const uint64_t off = nd.cand_off;
         const uint32_t level = nd.level;
         const uint64_t morton = nd.morton;
@@ -299,24 +308,34 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
                 const uint64_t start = ns.start[c];
                 const uint32_t jbase = ns.prefix[c];
                 const uint32_t* src_lut = ((ns.kind >> c) & 1u) ? a.stage_lut : a.leaf_lut;
+                const uint16_t* src_rec = reinterpret_cast<const uint16_t*>(((ns.kind >> c) & 1u) ? a.stage_rec : a.leaf_rec);
                 for (uint32_t k = threadIdx.x; k < cnt; k += blockDim.x) {
                     if (*(volatile uint32_t*)&s_overflow) break;
                     const uint32_t j = jbase + k;
-                    const uint32_t idx = src_lut[start + k];
-                    Coord co[3];
-                    uint32_t col[3];
-                    load_point<kF32>(a.cloud + (uint64_t)idx * a.stride, co, col);
-                    float ux, uy, uz;
-                    int ix = axis_cell<kF32>(co[0], ax0, a.grid, ux);
-                    int iy = axis_cell<kF32>(co[1], ax1, a.grid, uy);
-                    int iz = axis_cell<kF32>(co[2], ax2, a.grid, uz);
+                    // cell from the record's quantised coordinates; the cloud point
+                    // is read only when a quantisation step straddles a boundary
+                    const uint16_t* rec = src_rec + (start + k) * 9;
+                    const int32_t q0 = rec_coord(rec, 0), q1 = rec_coord(rec, 1), q2 = rec_coord(rec, 2);
+                    int ix = quant_cell(q0, qa0, a.grid);
+                    int iy = quant_cell(q1, qa1, a.grid);
+                    int iz = quant_cell(q2, qa2, a.grid);
                     if ((ix | iy | iz) < 0) {
-                        atomicOr(a.err, kErrBelowBox);
-                        ix = max(ix, 0);
-                        iy = max(iy, 0);
-                        iz = max(iz, 0);
+                        const uint32_t idx = src_lut[start + k];
+                        Coord co[3];
+                        uint32_t col[3];
+                        load_point<kF32>(a.cloud + (uint64_t)idx * a.stride, co, col);
+                        float u;
+                        if (ix < 0) ix = axis_cell<kF32>(co[0], ax0, a.grid, u);
+                        if (iy < 0) iy = axis_cell<kF32>(co[1], ax1, a.grid, u);
+                        if (iz < 0) iz = axis_cell<kF32>(co[2], ax2, a.grid, u);
+                        if ((ix | iy | iz) < 0) {
+                            atomicOr(a.err, kErrBelowBox);
+                            ix = max(ix, 0);
+                            iy = max(iy, 0);
+                            iz = max(iz, 0);
+                        }
                     }
-                    uint32_t b = ((uint32_t)ix >> 2) + bm.bs * (((uint32_t)iy >> 2) + bm.bs * ((uint32_t)iz >> 2));
+                    uint32_t b = ((uint32_t)ix >> 2) | (((uint32_t)iy >> 2) << 8) | (((uint32_t)iz >> 2) << 16);
                     uint32_t bit = (ix & 3) | ((iy & 3) << 2) | ((iz & 3) << 4);
                     bool fresh;
                     uint32_t slot = brick_insert(bm, b + 1, fresh);
@@ -328,9 +347,9 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
                     atomicOr(reinterpret_cast<unsigned long long*>(&bm.mask[slot]), 1ull << bit);
                     a.key_cache[off + j] = (slot << 6) | bit;
                     if (weighted) {
-                        a.unit_cache[(off + j) * 3 + 0] = ux;
-                        a.unit_cache[(off + j) * 3 + 1] = uy;
-                        a.unit_cache[(off + j) * 3 + 2] = uz;
+                        a.unit_cache[(off + j) * 3 + 0] = quant_units(q0, qa0);
+                        a.unit_cache[(off + j) * 3 + 1] = quant_units(q1, qa1);
+                        a.unit_cache[(off + j) * 3 + 2] = quant_units(q2, qa2);
                     }
                 }
             }
@@ -366,6 +385,16 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
             if (threadIdx.x == 0) ns.cells = total;
         }
         __syncthreads();
+        // rank -> (brick slot, bit), for the per-cell emit
+        for (uint32_t k = threadIdx.x; k < bm.cap; k += blockDim.x) {
+            uint64_t m = bm.mask[k];
+            uint32_t r = bm.base[k];
+            while (m) {
+                const uint32_t bit = (uint32_t)__ffsll((long long)m) - 1;
+                m &= m - 1;
+                a.cell_slot[off + r++] = (k << 6) | bit;
+            }
+        }
         const uint32_t cells = ns.cells;
         for (uint32_t r = threadIdx.x; r < cells; r += blockDim.x) {
             a.acc_best[off + r] = ~0ull;
@@ -383,22 +412,43 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
             const uint32_t* src_lut = staged ? a.stage_lut : a.leaf_lut;
             const uint8_t* src_rec = staged ? a.stage_rec : a.leaf_rec;
             for (uint32_t k = threadIdx.x; k < cnt; k += blockDim.x) {
-                uint32_t kc = a.key_cache[off + jbase + k];
-                uint32_t slot = kc >> 6, bit = kc & 63;
-                uint32_t rank = bm.base[slot] + (uint32_t)__popcll(bm.mask[slot] & ((1ull << bit) - 1ull));
-                uint32_t idx = src_lut[start + k];
-                uint64_t key = idx;
-                if constexpr (random) key |= (uint64_t)rp_priority(a.seed, level, morton, idx) << 32;
+                const uint32_t kc = a.key_cache[off + jbase + k];
+                const uint32_t slot = kc >> 6, bit = kc & 63;
+                const uint32_t rank = bm.base[slot] + (uint32_t)__popcll(bm.mask[slot] & ((1ull << bit) - 1ull));
+                const uint32_t idx = src_lut[start + k];
+                // first point: (cloud index, candidate) -- the smallest index wins and
+                // carries its candidate position; explicit random: (priority, index)
+                uint64_t key;
+                if constexpr (random) key = ((uint64_t)rp_priority(a.seed, level, morton, idx) << 32) | idx;
+                else key = ((uint64_t)idx << 32) | (jbase + k);
                 atomicMin(reinterpret_cast<unsigned long long*>(&a.acc_best[off + rank]), (unsigned long long)key);
                 if (averaged && !weighted) {
                     const uint16_t* src = reinterpret_cast<const uint16_t*>(src_rec + (start + k) * 18);
-                    uint64_t enc = encode_colors(src[6], src[7], src[8]);
+                    const uint64_t enc = encode_colors(src[6], src[7], src[8]);
                     atomicAdd(reinterpret_cast<unsigned long long*>(&a.acc_intra[off + rank]), (unsigned long long)enc);
                 }
                 if (weighted) atomicAdd(&a.csr_count[off + rank], 1u);
             }
         }
         __syncthreads();
+
+        // ---- explicit random: the candidate holding each cell's winning key
+        if constexpr (random) {
+            for (uint32_t c = 0; c < ns.nchild; ++c) {
+                const uint32_t cnt = ns.count[c];
+                const uint64_t start = ns.start[c];
+                const uint32_t jbase = ns.prefix[c];
+                const uint32_t* src_lut = ((ns.kind >> c) & 1u) ? a.stage_lut : a.leaf_lut;
+                for (uint32_t k = threadIdx.x; k < cnt; k += blockDim.x) {
+                    uint32_t kc = a.key_cache[off + jbase + k];
+                    uint32_t slot = kc >> 6, bit = kc & 63;
+                    uint32_t rank = bm.base[slot] + (uint32_t)__popcll(bm.mask[slot] & ((1ull << bit) - 1ull));
+                    uint32_t idx = src_lut[start + k];
+                    if ((uint32_t)a.acc_best[off + rank] == idx) a.acc_sel[off + rank] = jbase + k;
+                }
+            }
+            __syncthreads();
+        }
 
         // ---- weighted: group candidates by cell (CSR)
         if (weighted) {
@@ -440,31 +490,25 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
 
         // ---- emit one record per occupied cell (thread per cell, rank order)
         for (uint32_t r = threadIdx.x; r < cells; r += blockDim.x) {
-            // slot holding rank r: the last slot whose base is <= r (bases are
-            // non-decreasing; the next non-empty slot starts above r)
-            uint32_t lo = 0, hi = bm.cap - 1;
-            while (lo < hi) {
-                uint32_t mid = (lo + hi + 1) >> 1;
-                if (bm.base[mid] <= r) lo = mid;
-                else hi = mid - 1;
-            }
-            const uint32_t slot = lo;
-            const uint64_t mk = bm.mask[slot];
-            const uint32_t want = r - bm.base[slot];
-            if (want >= (uint32_t)__popcll(mk)) {
-                atomicOr(a.err, kErrProbe);
-                continue;
-            }
-            const uint32_t bit = nth_set_bit(mk, want);
+            const uint32_t ks = a.cell_slot[off + r];
+            const uint32_t slot = ks >> 6, bit = ks & 63;
             const uint32_t brick = bm.key[slot] - 1;
-            const int bx = (int)(brick % bm.bs), by = (int)((brick / bm.bs) % bm.bs), bz = (int)(brick / (bm.bs * bm.bs));
+            const int bx = (int)(brick & 0xFF), by = (int)((brick >> 8) & 0xFF), bz = (int)(brick >> 16);
             const int lx = (int)(bit & 3), ly = (int)((bit >> 2) & 3), lz = (int)((bit >> 4) & 3);
             const uint64_t best = a.acc_best[off + r];
-            const uint32_t idx = (uint32_t)best;
-            Coord co[3];
-            uint32_t col[3];
-            load_point<kF32>(a.cloud + (uint64_t)idx * a.stride, co, col);
-            uint16_t cr = (uint16_t)col[0], cg = (uint16_t)col[1], cb = (uint16_t)col[2];
+            const uint32_t idx = random ? (uint32_t)best : (uint32_t)(best >> 32);
+            const uint32_t jsel = random ? a.acc_sel[off + r] : (uint32_t)best;
+            // the winner's record holds its output coordinates (same cloud
+            // minimum and scale at every level) and, unaveraged, its colour
+            uint32_t csel = 0;
+            while (csel + 1 < ns.nchild && ns.prefix[csel + 1] <= jsel) ++csel;
+            const uint64_t spos = ns.start[csel] + (jsel - ns.prefix[csel]);
+            const uint16_t* srec =
+                reinterpret_cast<const uint16_t*>((((ns.kind >> csel) & 1u) ? a.stage_rec : a.leaf_rec) + spos * 18);
+            uint16_t rw[9];
+#pragma unroll
+            for (int q = 0; q < 9; ++q) rw[q] = srec[q];
+            uint16_t cr = rw[6], cg = rw[7], cb = rw[8];
             if (intra) {
                 decode_colors(a.acc_intra[off + r], cr, cg, cb);
             } else if (inter && !weighted) {
@@ -481,12 +525,13 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
                     cb = (uint16_t)(f.sb / f.sw);
                 }
             }
-            int32_t ox_ = out_coord<kF32>(co[0], a.out.ax[0]);
-            int32_t oy_ = out_coord<kF32>(co[1], a.out.ax[1]);
-            int32_t oz_ = out_coord<kF32>(co[2], a.out.ax[2]);
-            if (ox_ == kCoordError || oy_ == kCoordError || oz_ == kCoordError) atomicOr(a.err, kErrCoordRange);
             a.out_lut[off + r] = idx;
-            store_record(a.out_rec, off + r, ox_, oy_, oz_, cr, cg, cb);
+            uint16_t* dst = reinterpret_cast<uint16_t*>(a.out_rec + (off + r) * 18);
+#pragma unroll
+            for (int q = 0; q < 6; ++q) dst[q] = rw[q];
+            dst[6] = cr;
+            dst[7] = cg;
+            dst[8] = cb;
         }
         if (threadIdx.x == 0) a.out_points[ni] = cells;
         __syncthreads();

@@ -5,6 +5,7 @@
 
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdint>
 
 #include "device_common.cuh"
@@ -22,11 +23,32 @@ struct OutParams {
     OutAxis ax[3];
 };
 
+// Cell position of a candidate from its quantised output coordinate q
+// (q = floor((p - cloud_min) / scale), the record's int32 coordinate):
+// u = (q - qn + theta) * B + base, theta in [0, 1), exact to rounding.
+struct QAxis {
+    int32_t qn;     // quantised coordinate of the node's bbox minimum
+    float base;     // ((cloud_min - node_min) + qn * scale) / t
+    float B;        // scale / t: width of one quantisation step in cells
+};
+
+// node_min, cloud_min: bbox minima; sf = 1/scale; t = node side / S.
+inline QAxis make_qaxis(double node_min, double cloud_min, double sf, double t) {
+    QAxis q;
+    double qn = std::floor((node_min - cloud_min) * sf);
+    q.qn = (int32_t)qn;
+    double base = ((cloud_min - node_min) + (double)q.qn / sf) / t;
+    q.base = (float)base;
+    q.B = (float)(1.0 / (sf * t));
+    return q;
+}
+
 // One internal node to subsample.  Children are listed in slot order; each
 // child's points are records [start, start + count) of either the leaf data
 // arrays (kind 0) or the internal staging arrays (kind 1).
 struct SubNode {
     AxisGrid ax[3];
+    QAxis qa[3];
     uint64_t morton;
     uint64_t cand_off;   // first candidate slot of this node in the level scratch
     uint64_t child_start[8];
@@ -63,6 +85,8 @@ struct SubLevelArgs {
     uint32_t* key_cache;        // per candidate: brick slot << 6 | bit
     float* unit_cache;          // per candidate: cell-unit position (weighted only)
     uint64_t* acc_best;         // per cell: selection key
+    uint32_t* acc_sel;          // per cell: winning candidate (explicit random)
+    uint32_t* cell_slot;        // per cell: brick slot holding it
     uint64_t* acc_intra;        // per cell: packed colour sum
     uint64_t* acc_inter;        // per cell: packed colour sum over the 3x3x3 neighbourhood
     uint64_t* acc_w;            // per cell: 4 x fixed-point weighted sums (weighted only)

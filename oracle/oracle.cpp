@@ -40,8 +40,9 @@
 //
 // The exact cell / coordinate formulas are evaluated directly in double here.
 // The only fp32 quantity the oracle shares with the GPU path is the cell-unit
-// position used by distance weighting (approx_cell_units), which is part of the
-// canonical definition of the weighted mode.
+// position used by distance weighting (quant_units: the centre of the point's
+// quantisation step in the node's grid), which is part of the canonical
+// definition of the weighted mode.
 
 #include <algorithm>
 #include <array>
@@ -209,57 +210,29 @@ inline int32_t ref_out_coord(double p, double mn, double sf) {
 // ---------------------------------------------------------------------------
 // Shared canonical pieces (must match the GPU path bit for bit).
 
-// Split of a coordinate into two floats: hi = value with its binary64 mantissa
-// truncated to 24 bits, lo = float(value - hi).  Returns false when the
-// exponent range is not handled by the fast path.
-inline bool split_coord(double p, uint32_t type, float* hi, float* lo) {
-    if (type == 0) {
-        *hi = (float)p;
-        *lo = 0.0f;
-        return true;
-    }
-    uint64_t bits;
-    std::memcpy(&bits, &p, 8);
-    uint32_t e = (uint32_t)((bits >> 52) & 0x7FF);
-    uint64_t mant = bits & ((1ull << 52) - 1);
-    if (e == 0 && mant == 0) {
-        *hi = (float)p;
-        *lo = 0.0f;
-        return true;
-    }
-    int ue = (int)e - 1023;
-    if (ue < -60 || ue > 100) return false;
-    uint64_t hb = bits & ~((1ull << 29) - 1);
-    double hd;
-    std::memcpy(&hd, &hb, 8);
-    *hi = (float)hd;
-    *lo = (float)(p - hd);
-    return true;
-}
-
-struct AxisApprox {
-    float m_hi, m_lo, r;
+// Quantised-coordinate parameters of one node axis: qn = quantised coordinate
+// of the node minimum, base = ((cloud_min - node_min) + qn / sf) / t and
+// B = 1 / (sf t) rounded to float; evaluated in this operation order.
+struct QAx {
+    int32_t qn;
+    float base;
+    float B;
 };
 
-inline AxisApprox make_axis(double mn, double t) {
-    AxisApprox a;
-    a.m_hi = (float)mn;
-    a.m_lo = (float)(mn - (double)a.m_hi);
-    a.r = (float)(1.0 / t);
-    return a;
+inline QAx make_qax(double node_min, double cloud_min, double sf, double t) {
+    QAx q;
+    double qn = std::floor((node_min - cloud_min) * sf);
+    q.qn = (int32_t)qn;
+    double base = ((cloud_min - node_min) + (double)q.qn / sf) / t;
+    q.base = (float)base;
+    q.B = (float)(1.0 / (sf * t));
+    return q;
 }
 
-// Cell-unit position (p - min) / t evaluated in fp32 from the split pieces.
-// Used only by distance weighting.  When the split is not available the exact
-// double quotient rounded to float is used.
-inline float approx_cell_units(double p, uint32_t type, double mn, double t, const AxisApprox& ax) {
-    float ph, pl;
-    if (!split_coord(p, type, &ph, &pl)) return (float)((p - mn) / t);
-    volatile float s = ph - ax.m_hi;
-    volatile float q = pl - ax.m_lo;
-    volatile float d = s + q;
-    volatile float a = d * ax.r;
-    return a;
+// Cell-unit position of a point with quantised coordinate q (its output
+// record coordinate): the centre of its quantisation step, in fp32.
+inline float quant_units(int32_t q, const QAx& a) {
+    return std::fmaf((float)(q - a.qn) + 0.5f, a.B, a.base);
 }
 
 // exp(x) for x in [-15, 0]: Cody & Waite range reduction x = k*ln2 + f with
@@ -639,7 +612,8 @@ Result* build(const uint8_t* cloud, const OracleParams& P) {
             const TNode& v = nodes[vi];
             const double side = cubic / std::pow(2.0, (double)(depth - v.level));   // fp_subsampling.cu:16-17
             const double t = side / Sg;                                           // kernel_helpers.cuh:14
-            AxisApprox ax[3] = {make_axis(v.mn[0], t), make_axis(v.mn[1], t), make_axis(v.mn[2], t)};
+            QAx qa[3] = {make_qax(v.mn[0], P.bb_min[0], sf[0], t), make_qax(v.mn[1], P.bb_min[1], sf[1], t),
+                         make_qax(v.mn[2], P.bb_min[2], sf[2], t)};
             std::vector<Cand> cands;
             cands.reserve(v.sub_count);
             for (int s = 0; s < 8; ++s) {
@@ -679,7 +653,7 @@ Result* build(const uint8_t* cloud, const OracleParams& P) {
                     cd.key = (uint32_t)(ix + iy * Sg + iz * (uint64_t)Sg * Sg);
                     if (weighted)
                         for (int a = 0; a < 3; ++a)
-                            cd.u[a] = approx_cell_units(p[a], P.cloud_type, v.mn[a], t, ax[a]);
+                            cd.u[a] = quant_units(ref_out_coord(p[a], P.bb_min[a], sf[a]), qa[a]);
                     cands.push_back(cd);
                 }
             }
