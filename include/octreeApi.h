@@ -117,4 +117,57 @@ OCPI_EXPORT int ocpi_get_level_counts(void* session, uint32_t level, uint32_t* o
  * values and their names (comma separated) into names (size name_bytes). */
 OCPI_EXPORT int ocpi_get_timings(void* session, double* ms, int max, char* names, int name_bytes, int* count);
 
+/* ---- allocation-free node subsampling (no counterpart in the reference) --
+ *
+ * For callers that may not allocate device memory: a plug-in living inside an
+ * application whose memory pool owns the whole GPU, or a pipeline that keeps
+ * every buffer in a fixed arena.  The session entry points above size and
+ * cudaMalloc their buffers; this one subsamples ONE octree node (the
+ * per-node step of ocpi_generate_octree) in a fixed scratch array that is
+ * part of the library's device image.  It calls no cudaMalloc, cudaFree or
+ * allocating library routine.
+ *
+ * Limits and sharing:
+ *   - at most OCPI_NOALLOC_MAX_CANDIDATES candidate points per call; larger
+ *     nodes are rejected with -1 and a message in ocpi_last_error();
+ *   - the scratch (OCPI_NOALLOC_SCRATCH_BYTES, 12.5 MiB) is held on every GPU
+ *     where this library's subsampling module is loaded, until process exit;
+ *   - every call shares the scratch and it keeps the last call's contents;
+ *     calls that overlap on the GPU (other streams, other host threads) race
+ *     and must be ordered by the caller;
+ *   - the first call on a device looks up the scratch address on that device
+ *     (cudaGetSymbolAddress, with the device current) and may load the
+ *     module: make that first call before any stream capture.
+ *
+ * All pointers named d* / device arrays are device memory of the current
+ * device; the call is asynchronous on `stream` (a cudaStream_t, NULL = the
+ * legacy default stream).
+ *   cloud             device: the point cloud (interleaved records of
+ *                     dataStride bytes), readable for 16 bytes past the last
+ *                     record
+ *   scale, cloudMin   host, 3 doubles: cloud scale and bounding-box minimum
+ *   nodeMin, nodeSide host: the node's bounding-box minimum and cube side
+ *   level, mortonKey  node level (0 = finest) and its Morton key in the level
+ *                     (used by random subsampling)
+ *   modeFlags         OCPI_SUB_* bits, as ocpi_configure_subsampling selects
+ *   candidateLut      device: cloud index of every candidate point
+ *   candidateRecords  device: the candidates' 18-byte octree.bin records
+ *   outLut, outRecords device: room for candidateCount entries / records
+ *   outStatus         device, 2 words: [0] points written, [1] error bits
+ *                     (1 point below the node box, 4 brick table overflow)
+ */
+#define OCPI_NOALLOC_MAX_CANDIDATES (131072u)
+#define OCPI_NOALLOC_SCRATCH_BYTES (13108480u)
+#define OCPI_SUB_INTRA (1u)
+#define OCPI_SUB_INTER (2u)
+#define OCPI_SUB_RANDOM (8u)
+#define OCPI_SUB_WEIGHTING (16u)
+OCPI_EXPORT int ocpi_subsample_node_noalloc(const uint8_t* cloud, uint8_t cloudType, uint32_t dataStride,
+                                            const double* scale, const double* cloudMin, const double* nodeMin,
+                                            double nodeSide, uint32_t level, uint64_t mortonKey,
+                                            uint32_t subsamplingGrid, uint32_t modeFlags, uint64_t seed,
+                                            const uint32_t* candidateLut, const uint8_t* candidateRecords,
+                                            uint32_t candidateCount, uint32_t* outLut, uint8_t* outRecords,
+                                            uint32_t* outStatus, void* stream);
+
 #endif /* OCTREE_API_H */

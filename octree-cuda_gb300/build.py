@@ -18,7 +18,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["k_chunking.cu", "k_subsample.cu"]
+CU_SOURCES = ["k_chunking.cu", "k_subsample.cu", "noalloc.cu"]
 CPP_SOURCES = ["builder.cpp", "export.cpp", "octree_api.cpp"]
 HEADERS = ["device_common.cuh", "kernels.h", "builder.h"]
 

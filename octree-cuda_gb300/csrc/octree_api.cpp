@@ -76,6 +76,14 @@ int execute(F&& fn) {
 
 }   // namespace
 
+namespace oc {
+// Records the message returned by ocpi_last_error() on this host thread.
+void set_last_error(const std::string& msg) {
+    g_last_error = msg;
+    if (g_log_level <= 3) std::fprintf(stderr, "[octree-gb300] error: %s\n", msg.c_str());
+}
+}   // namespace oc
+
 extern "C" {
 
 int ocpi_set_logging_level(int level) {

@@ -29,13 +29,18 @@ REFERENCE_SYMBOLS = [
 ADDED_SYMBOLS = [
     "ocpi_last_error", "ocpi_set_random_seed", "ocpi_set_debug_flags", "ocpi_get_stats",
     "ocpi_get_node_count", "ocpi_get_hierarchy", "ocpi_get_records", "ocpi_get_lut",
-    "ocpi_get_level_counts", "ocpi_get_timings",
+    "ocpi_get_level_counts", "ocpi_get_timings", "ocpi_subsample_node_noalloc",
 ]
 
 HIER_DTYPE = np.dtype([("type", "u1"), ("mask", "u1"), ("points", "<u4"),
                        ("byte_offset", "<u8"), ("byte_size", "<u8")])
 RECORD_DTYPE = np.dtype([("x", "<i4"), ("y", "<i4"), ("z", "<i4"),
                          ("r", "<u2"), ("g", "<u2"), ("b", "<u2")])
+
+
+# ocpi_subsample_node_noalloc: mode bits and the fixed scratch limit
+SUB_INTRA, SUB_INTER, SUB_RANDOM, SUB_WEIGHTING = 1, 2, 8, 16
+NOALLOC_MAX_CANDIDATES = 131072
 
 
 class OctreeError(RuntimeError):
@@ -99,6 +104,8 @@ def load_library(path=LIB_PATH):
         "ocpi_get_level_counts": [vp, u32, vp],
         "ocpi_get_timings": [vp, ctypes.POINTER(ctypes.c_double), ctypes.c_int, ctypes.c_char_p, ctypes.c_int,
                              ctypes.POINTER(ctypes.c_int)],
+        "ocpi_subsample_node_noalloc": [vp, u8, u32, ctypes.POINTER(d), ctypes.POINTER(d), ctypes.POINTER(d), d,
+                                        u32, u64, u32, u32, u64, vp, vp, u32, vp, vp, vp, vp],
     }
     for name, args in sig.items():
         fn = getattr(L, name)

@@ -42,3 +42,13 @@ def test_errors_are_return_codes():
 def test_python_session_raises():
     with pytest.raises(octree_api.OctreeError):
         octree_api._check(-1, "probe")
+
+
+def test_noalloc_rejects_oversized_node_without_gpu():
+    # the size limit is checked before any CUDA call
+    L = octree_api.load_library()
+    n = octree_api.NOALLOC_MAX_CANDIDATES + 1
+    rc = L.ocpi_subsample_node_noalloc(None, 1, 27, None, None, None, 1.0, 0, 0, 32, 0, 0, None, None, n, None,
+                                       None, None, None)
+    assert rc == -1
+    assert b"exceed the fixed scratch limit" in L.ocpi_last_error()
