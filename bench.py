@@ -118,7 +118,7 @@ def stage_bytes(st, n, stride, timings):
     return {
         "count": n * stride,
         "distribute": n * stride + n * (4 + 18),
-        "subsample": p_in * (4 + stride + 6) + p_out * (4 + 18),
+        "subsample": p_in * (4 + stride) + p_out * (4 + 18),
     }
 
 

@@ -81,6 +81,45 @@ void upload_vec(DevBuf& b, const std::vector<T>& v, cudaStream_t s) {
 
 }   // namespace
 
+// Reference cell formula of one axis (mapPointToGrid, kernel_helpers.cuh:14-24)
+// evaluated in binary64 on the host: -1 below the bounding box.
+static int host_cell(double p, double mn, double t, uint32_t grid) {
+    const double u = (p - mn) / t;
+    const double v = std::fmin(u, (double)grid - 1.0);
+    if (!(v > -1.0)) return -1;
+    return (int)(long long)v;
+}
+
+// The cell is a non-decreasing function of the coordinate, hence of its
+// ordered key: each boundary is found by bisection over the keys.
+void make_cell_keys64(double mn, double t, uint32_t grid, int64_t* keys) {
+    const int64_t kmin = host_key64(-INFINITY), kmax = host_key64(INFINITY);
+    for (uint32_t i = 0; i < grid; ++i) {
+        int64_t lo = kmin, hi = kmax;   // host_cell(+inf) = grid - 1 >= i
+        while (lo < hi) {
+            const int64_t mid = lo + (int64_t)(((uint64_t)hi - (uint64_t)lo) / 2);
+            if (host_cell(host_from_key64(mid), mn, t, grid) >= (int)i) hi = mid;
+            else lo = mid + 1;
+        }
+        keys[i] = lo;
+    }
+    keys[grid] = keys[grid + 1] = INT64_MAX;
+}
+
+void make_cell_keys32(double mn, double t, uint32_t grid, int32_t* keys) {
+    const int32_t kmin = host_key32(-INFINITY), kmax = host_key32(INFINITY);
+    for (uint32_t i = 0; i < grid; ++i) {
+        int32_t lo = kmin, hi = kmax;
+        while (lo < hi) {
+            const int32_t mid = lo + (int32_t)(((uint32_t)hi - (uint32_t)lo) / 2);
+            if (host_cell((double)host_from_key32(mid), mn, t, grid) >= (int)i) hi = mid;
+            else lo = mid + 1;
+        }
+        keys[i] = lo;
+    }
+    keys[grid] = keys[grid + 1] = INT32_MAX;
+}
+
 Builder::Builder(const BuildConfig& cfg, const uint8_t* host_cloud, int device) : cfg_(cfg), device_(device) {
     cfg_.validate();
     check_cuda(cudaSetDevice(device_), "cudaSetDevice");
@@ -112,6 +151,26 @@ Builder::Builder(const BuildConfig& cfg, const uint8_t* host_cloud, int device) 
     child_first_.ensure((size_t)node_cap_ * 4);
     level_start_.ensure((depth_ + 2) * 4);
     n_nodes_.ensure(4);
+    {
+        // exact boundary keys of the chunking grid and the Morton spread table
+        const uint32_t G = cfg_.chunk_grid;
+        const double t0 = (cfg_.bb_max[0] - cfg_.bb_min[0]) / G;   // kernel_helpers.cuh:14
+        std::vector<uint32_t> sp(G);
+        for (uint32_t i = 0; i < G; ++i) sp[i] = spread3(i);
+        if (cfg_.cloud_type == 0) {
+            std::vector<int32_t> k(3 * (G + 2));
+            for (int a = 0; a < 3; ++a) make_cell_keys32(cfg_.bb_min[a], t0, G, k.data() + a * (G + 2));
+            cell_keys_.ensure(k.size() * 4);
+            check_cuda(cudaMemcpy(cell_keys_.p, k.data(), k.size() * 4, cudaMemcpyHostToDevice), "H2D keys");
+        } else {
+            std::vector<int64_t> k(3 * (G + 2));
+            for (int a = 0; a < 3; ++a) make_cell_keys64(cfg_.bb_min[a], t0, G, k.data() + a * (G + 2));
+            cell_keys_.ensure(k.size() * 8);
+            check_cuda(cudaMemcpy(cell_keys_.p, k.data(), k.size() * 8, cudaMemcpyHostToDevice), "H2D keys");
+        }
+        spread_.ensure(G * 4);
+        check_cuda(cudaMemcpy(spread_.p, sp.data(), G * 4, cudaMemcpyHostToDevice), "H2D spread");
+    }
     cloud_.ensure((size_t)cfg_.n * cfg_.stride + 64);
     lut_.ensure((size_t)cfg_.n * 4);
     rec_.ensure((size_t)cfg_.n * 18);
@@ -167,6 +226,7 @@ void Builder::check_device_errors(const char* stage) {
     if (e & kErrProbe) throw Error(std::string(stage) + ": subsampling brick table overflow");
     if (e & kErrCapacity) throw Error(std::string(stage) + ": node capacity exceeded");
     if (e & kErrTag) throw Error(std::string(stage) + ": a point found no leaf");
+    if (e & kErrTimeout) throw Error(std::string(stage) + ": a bulk copy did not complete in time");
 }
 
 void Builder::generate() {
@@ -174,7 +234,13 @@ void Builder::generate() {
     CloudGrid g;
     g.grid = cfg_.chunk_grid;
     const double t0 = cubic / cfg_.chunk_grid;   // kernel_helpers.cuh:14
-    for (int a = 0; a < 3; ++a) g.ax[a] = make_axis(cfg_.bb_min[a], t0);
+    for (int a = 0; a < 3; ++a) {
+        g.ax[a] = make_axis(cfg_.bb_min[a], t0);
+        g.r[a] = (float)(1.0 / t0);
+        g.c[a] = (float)(-cfg_.bb_min[a] / t0);
+    }
+    g.keys = cell_keys_.p;
+    g.spread = spread_.as<uint32_t>();
     OutParams op;
     for (int a = 0; a < 3; ++a) op.ax[a] = make_out_axis(cfg_.bb_min[a], 1.0 / cfg_.scale[a]);   // octree_chunking.cu:109-111
     const bool f32 = cfg_.cloud_type == 0;
@@ -228,9 +294,11 @@ void Builder::generate() {
     check_cuda(cudaMemsetAsync(fill_.p, 0, nodes_.size() * 4, stream_), "memset");
     launches_ += launch_tag_leaves(pyr_.as<uint32_t>(), loff_.as<uint64_t>(), leaves_.as<uint32_t>(), (uint32_t)leaf_ids_.size(),
                       key_.as<uint32_t>(), level_.as<uint8_t>(), stream_);
+    launches_ += launch_push_tags(pyr_.as<uint32_t>(), loff_.as<uint64_t>(), depth_, cfg_.chunk_grid,
+                                  err_.as<uint32_t>(), stream_);
     launches_ += launch_distribute(cloud_.as<uint8_t>(), cfg_.n, cfg_.stride, f32, g, op, pyr_.as<uint32_t>(),
-                      loff_.as<uint64_t>(), depth_, data_idx_.as<uint64_t>(), fill_.as<uint32_t>(),
-                      lut_.as<uint32_t>(), rec_.as<uint8_t>(), err_.as<uint32_t>(), num_sms_, stream_);
+                                   data_idx_.as<uint64_t>(), fill_.as<uint32_t>(), lut_.as<uint32_t>(),
+                                   rec_.as<uint8_t>(), err_.as<uint32_t>(), num_sms_, stream_);
     stage_mark("distribute");
     check_cuda(cudaGetLastError(), "launch");
 

@@ -130,6 +130,7 @@ private:
     DevBuf key_cache_, unit_cache_, acc_best_, acc_sel_, cell_slot_, acc_intra_, acc_w_, csr_count_, csr_start_, csr_pts_;
     DevBuf place_src_, place_dst_, place_cnt_;
     DevBuf g_key_, g_mask_, g_base_;   // per-block global brick tables
+    DevBuf cell_keys_, spread_;         // chunking-grid boundary keys and Morton spread table
     uint32_t launches_ = 0;
     size_t place_count_ = 0;
     bool lut_placed_ = false;

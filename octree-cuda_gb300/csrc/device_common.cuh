@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstring>
 
 namespace oc {
 
@@ -123,7 +124,41 @@ enum : uint32_t {
     kErrProbe = 1u << 2,         // a hash probe exceeded its bound
     kErrCapacity = 1u << 3,      // a scratch buffer was too small
     kErrTag = 1u << 4,           // a point found no leaf
+    kErrTimeout = 1u << 5,       // a bounded wait on a bulk copy gave up
 };
+
+// ---------------------------------------------------------------------------
+// Ordered keys: monotone maps of IEEE bit patterns onto signed integers, so
+// that binary64 / binary32 values compare exactly as integers (negative
+// values have their magnitude bits reversed).
+
+inline int64_t host_key64(double d) {
+    uint64_t b;
+    std::memcpy(&b, &d, 8);
+    return (int64_t)((b >> 63) ? (b ^ 0x7FFFFFFFFFFFFFFFull) : b);
+}
+
+inline double host_from_key64(int64_t k) {
+    uint64_t b = (uint64_t)k;
+    if (k < 0) b ^= 0x7FFFFFFFFFFFFFFFull;
+    double d;
+    std::memcpy(&d, &b, 8);
+    return d;
+}
+
+inline int32_t host_key32(float f) {
+    uint32_t b;
+    std::memcpy(&b, &f, 4);
+    return (int32_t)((b >> 31) ? (b ^ 0x7FFFFFFFu) : b);
+}
+
+inline float host_from_key32(int32_t k) {
+    uint32_t b = (uint32_t)k;
+    if (k < 0) b ^= 0x7FFFFFFFu;
+    float f;
+    std::memcpy(&f, &b, 4);
+    return f;
+}
 
 #if defined(__CUDACC__)
 // ===== device-only arithmetic =====
@@ -384,6 +419,110 @@ __device__ __forceinline__ void load_point(const uint8_t* rec, Coord c[3], uint3
         col[1] = (uint32_t)(r3 >> 8) & 0xFF;
         col[2] = (uint32_t)(r3 >> 16) & 0xFF;
     }
+}
+
+// ---------------------------------------------------------------------------
+// Ordered keys on the device (same maps as host_key64 / host_key32).
+
+__device__ __forceinline__ long long dev_key64(uint32_t lo, uint32_t hi) {
+    const uint32_t s = (uint32_t)((int32_t)hi >> 31);
+    return (long long)(((uint64_t)(hi ^ (s >> 1)) << 32) | (uint64_t)(lo ^ s));
+}
+
+__device__ __forceinline__ int dev_key32(uint32_t b) {
+    return (int)(b ^ ((uint32_t)((int32_t)b >> 31) >> 1));
+}
+
+// A float close to the binary64 value hi:lo (mantissa truncated to 24 bits);
+// meaningless outside the binary32 exponent range, which only makes the cell
+// estimate below miss and fall back to the exact path.
+__device__ __forceinline__ float approx_f64(uint32_t lo, uint32_t hi) {
+    const uint32_t t = hi - (896u << 20);
+    return __uint_as_float((__funnelshift_l(lo, t, 3) & 0x7FFFFFFFu) | (hi & 0x80000000u));
+}
+
+// Cell index of one axis from exact boundary keys: keys[i] is the least key
+// whose cell is >= i (keys[grid] = keys[grid + 1] = the largest key), so the
+// cell of `key` is the i with keys[i] <= key < keys[i + 1].  `est` is an
+// approximate cell-unit position; the estimate and its two neighbours are
+// checked.  Returns -2 when none matches (the caller evaluates the cell
+// exactly).
+template <typename K>
+__device__ __forceinline__ int table_cell(K key, float est, const K* keys, uint32_t grid) {
+    const float e = fminf(fmaxf(est, 0.0f), (float)(grid - 1));   // NaN -> 0
+    const int i = __float_as_int(__fadd_rd(e, 8388608.0f)) - 0x4B000000;   // floor(e)
+    const K lo = keys[i], hi = keys[i + 1];
+    if (key >= lo && key < hi) return i;
+    if (key < lo) return (i > 0 && key >= keys[i - 1]) ? i - 1 : -2;
+    return key < keys[i + 2] ? i + 1 : -2;
+}
+
+// ---------------------------------------------------------------------------
+// Bulk (TMA) copies into shared memory, completed on an mbarrier.
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_barrier_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// dst, src 16-byte aligned; bytes a multiple of 16.
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Waits for the phase with parity `parity`; gives up after about 2^31 clock
+// cycles (about a second) and returns false.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity))
+        if (clock64() - t0 > (1ll << 31)) return false;
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// Runs: consecutive lanes of a warp holding the same key.  All 32 lanes must
+// call these together.
+
+__device__ __forceinline__ uint32_t run_starts(uint32_t key) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t prev = __shfl_up_sync(0xffffffffu, key, 1);
+    return __ballot_sync(0xffffffffu, lane == 0 || prev != key);
+}
+
+// first lane of this lane's run
+__device__ __forceinline__ uint32_t run_leader(uint32_t starts) {
+    const uint32_t lane = threadIdx.x & 31;
+    return 31 - __clz(starts & (0xffffffffu >> (31 - lane)));
+}
+
+// one past the last lane of the run that starts at this lane
+__device__ __forceinline__ uint32_t run_end(uint32_t starts) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t higher = starts & ~(0xffffffffu >> (31 - lane));
+    return higher ? (uint32_t)__ffs(higher) - 1 : 32u;
 }
 
 #endif   // __CUDACC__

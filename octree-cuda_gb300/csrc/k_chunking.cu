@@ -12,6 +12,7 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <type_traits>
 
 #include "device_common.cuh"
 #include "kernels.h"
@@ -20,73 +21,191 @@ namespace oc {
 
 namespace {
 
-constexpr int kTilePoints = 2048;
-constexpr int kTileThreads = 512;
 constexpr uint32_t kLeafTag = 0x80000000u;
+constexpr uint32_t kNoKey = 0xFFFFFFFFu;   // run key of lanes without a point
 
 __device__ __forceinline__ void set_error(uint32_t* err, uint32_t bit) {
     atomicOr(err, bit);
 }
 
-// Copies the byte span of `cnt` records starting at record p0 into shared
-// memory with 16-byte vector loads; returns the offset of record p0 in smem.
-// The cloud buffer is padded so that rounding the span up to 16 bytes stays
-// inside the allocation.
-__device__ __forceinline__ uint32_t stage_tile(const uint8_t* __restrict__ cloud, uint64_t p0, uint32_t cnt,
-                                               uint32_t stride, uint4* smem) {
-    uint64_t b0 = p0 * stride, b1 = (p0 + cnt) * stride;
-    uint64_t a0 = b0 & ~15ull, a1 = (b1 + 15) & ~15ull;
-    uint32_t nvec = (uint32_t)((a1 - a0) >> 4);
-    const uint4* src = reinterpret_cast<const uint4*>(cloud + a0);
-    for (uint32_t v = threadIdx.x; v < nvec; v += blockDim.x) smem[v] = __ldg(src + v);
-    return (uint32_t)(b0 - a0);
+// ---------------------------------------------------------------------------
+// Tile pipeline of the two streaming passes over the cloud (counting and
+// distribution).  Each block walks tiles blockIdx.x, +gridDim.x, ... of
+// `tile` records; tile j+1 is bulk-copied (TMA) into the other of two
+// shared-memory buffers while tile j is processed.
+
+// counting: 1024-record tiles, 512 threads
+constexpr uint32_t kCountTile = 1024;
+constexpr uint32_t kCountThreads = 512;
+// distribution: 896-record tiles, 448 threads and a record staging area per
+// warp (three blocks fit one SM with float64 records)
+constexpr uint32_t kDistTile = 896;
+constexpr uint32_t kDistThreads = 448;
+constexpr uint32_t kStageBytes = 592;   // >= 2 + 32 * 18 + 2, 16-byte multiple
+
+__host__ __device__ inline uint32_t align_up(uint32_t x, uint32_t a) {
+    return (x + a - 1) / a * a;
 }
 
-template <bool kF32>
-__device__ __forceinline__ uint32_t point_cell(const uint8_t* rec, const CloudGrid& g, Coord c[3], uint32_t col[3],
-                                               bool& below) {
-    load_point<kF32>(rec, c, col);
-    float u;
-    int ix = axis_cell<kF32>(c[0], g.ax[0], g.grid, u);
-    int iy = axis_cell<kF32>(c[1], g.ax[1], g.grid, u);
-    int iz = axis_cell<kF32>(c[2], g.ax[2], g.grid, u);
-    below = (ix | iy | iz) < 0;
-    return below ? 0u : morton3((uint32_t)ix, (uint32_t)iy, (uint32_t)iz);
+// Shared-memory layout: [0, 16) two mbarriers, [16, 20) abort flag, then the
+// boundary keys of the three axes, the Morton spread table, the per-warp
+// staging areas and two tile buffers.  A buffer holds a tile's byte span
+// rounded out to 16 bytes plus read slack.
+struct ChunkSmem {
+    uint32_t keys_off, spread_off, stage_off, buf_off, buf_bytes, total;
+};
+
+__host__ __device__ inline ChunkSmem chunk_smem(uint32_t stride, uint32_t grid, bool f32, uint32_t tile,
+                                                uint32_t stage_bytes) {
+    ChunkSmem m;
+    m.keys_off = 128;
+    m.spread_off = align_up(m.keys_off + 3 * (grid + 2) * (f32 ? 4u : 8u), 16);
+    m.stage_off = align_up(m.spread_off + grid * 4, 128);
+    m.buf_off = align_up(m.stage_off + stage_bytes, 128);
+    m.buf_bytes = align_up(tile * stride + 48, 128);
+    m.total = m.buf_off + 2 * m.buf_bytes;
+    return m;
 }
 
+// Copies the boundary keys and the spread table into shared memory.
 template <bool kF32>
-__global__ void __launch_bounds__(kTileThreads) k_count(const uint8_t* __restrict__ cloud, uint64_t n, uint32_t stride,
-                                                        CloudGrid g, uint32_t* __restrict__ pyr0, uint32_t* err) {
-    extern __shared__ uint4 smem[];
-    const uint8_t* buf = reinterpret_cast<const uint8_t*>(smem);
-    const uint32_t lane = threadIdx.x & 31;
-    for (uint64_t tile = blockIdx.x; tile * kTilePoints < n; tile += gridDim.x) {
-        uint64_t p0 = tile * kTilePoints;
-        uint32_t cnt = (uint32_t)((n - p0) < (uint64_t)kTilePoints ? (n - p0) : (uint64_t)kTilePoints);
-        uint32_t shift = stage_tile(cloud, p0, cnt, stride, smem);
-        __syncthreads();
-        for (uint32_t base = 0; base < cnt; base += blockDim.x) {
-            uint32_t k = base + threadIdx.x;
-            bool valid = k < cnt;
-            uint32_t m = 0;
-            if (valid) {
-                Coord c[3];
-                uint32_t col[3];
-                bool below;
-                m = point_cell<kF32>(buf + shift + (uint64_t)k * stride, g, c, col, below);
-                if (below) {
-                    set_error(err, kErrBelowBox);
-                    valid = false;
-                }
-            }
-            unsigned active = __ballot_sync(0xffffffffu, valid);
-            if (valid) {
-                unsigned peers = __match_any_sync(active, m);
-                if ((int)lane == __ffs(peers) - 1) atomicAdd(&pyr0[m], (uint32_t)__popc(peers));
-            }
-        }
-        __syncthreads();
+__device__ __forceinline__ void load_tables(const CloudGrid& g, uint8_t* smem, const ChunkSmem& L) {
+    using K = typename std::conditional<kF32, int32_t, long long>::type;
+    const K* src = static_cast<const K*>(g.keys);
+    K* dst = reinterpret_cast<K*>(smem + L.keys_off);
+    for (uint32_t i = threadIdx.x; i < 3 * (g.grid + 2); i += blockDim.x) dst[i] = src[i];
+    uint32_t* sp = reinterpret_cast<uint32_t*>(smem + L.spread_off);
+    for (uint32_t i = threadIdx.x; i < g.grid; i += blockDim.x) sp[i] = g.spread[i];
+}
+
+__device__ __forceinline__ void issue_tile(const uint8_t* __restrict__ cloud, uint64_t n, uint32_t stride, uint32_t tile,
+                                           uint64_t t, uint8_t* buf, uint64_t* bar) {
+    const uint64_t p0 = t * tile;
+    const uint64_t p1 = (n - p0) < tile ? n : p0 + tile;
+    const uint64_t a0 = (p0 * stride) & ~15ull, a1 = (p1 * stride + 15) & ~15ull;
+    bulk_load(buf, cloud + a0, (uint32_t)(a1 - a0), bar);
+}
+
+// Runs body(records_of_tile, first_point, count) for every tile of this
+// block.  The body must be memory-safe for any buffer contents: after a
+// bounded wait gives up (error bit kErrTimeout) the tile is still processed
+// by every thread, so that warp collectives stay converged, and the loop
+// ends at the next block barrier.
+template <uint32_t kTile, class Body>
+__device__ __forceinline__ void tile_loop(const uint8_t* __restrict__ cloud, uint64_t n, uint32_t stride, uint8_t* smem,
+                                          const ChunkSmem& L, uint32_t* err, Body&& body) {
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
+    volatile uint32_t* abort_flag = reinterpret_cast<volatile uint32_t*>(smem + 16);
+    uint8_t* buf0 = smem + L.buf_off;
+    uint8_t* buf1 = buf0 + L.buf_bytes;
+    const uint64_t tiles = (n + kTile - 1) / kTile;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        *abort_flag = 0;
+        fence_barrier_init();
     }
+    __syncthreads();
+    uint64_t t = blockIdx.x;
+    if (threadIdx.x == 0 && t < tiles) issue_tile(cloud, n, stride, kTile, t, buf0, &bar[0]);
+    uint32_t j = 0;
+    bool aborted = false;
+    for (; t < tiles; t += gridDim.x, ++j) {
+        const uint32_t slot = j & 1;
+        const uint64_t tn = t + gridDim.x;
+        // the other buffer was released by the barrier that ended the previous tile
+        if (threadIdx.x == 0 && tn < tiles) issue_tile(cloud, n, stride, kTile, tn, slot ? buf0 : buf1, &bar[slot ^ 1]);
+        if (!mbar_wait_bounded(&bar[slot], (j >> 1) & 1)) {
+            set_error(err, kErrTimeout);
+            *abort_flag = 1;
+        }
+        const uint64_t p0 = t * kTile;
+        const uint32_t cnt = (uint32_t)((n - p0) < kTile ? (n - p0) : kTile);
+        body((slot ? buf1 : buf0) + (uint32_t)((p0 * stride) & 15), p0, cnt);
+        __syncthreads();
+        if (*abort_flag) {
+            aborted = true;
+            break;
+        }
+    }
+    if (aborted && threadIdx.x == 0) {
+        // let the copies still in flight land before the block exits (bounded)
+        const uint32_t slot = j & 1;
+        mbar_wait_bounded(&bar[slot], (j >> 1) & 1);
+        if (t + gridDim.x < tiles) mbar_wait_bounded(&bar[slot ^ 1], ((j + 1) >> 1) & 1);
+    }
+}
+
+// 32-bit words w[0..kWords) of a record at any byte alignment in shared memory.
+template <int kWords>
+__device__ __forceinline__ void record_words(const uint8_t* rec, uint32_t (&w)[kWords]) {
+    const uintptr_t a = reinterpret_cast<uintptr_t>(rec);
+    const uint32_t* q = reinterpret_cast<const uint32_t*>(a & ~(uintptr_t)3);
+    const uint32_t s = (uint32_t)(a & 3) * 8;
+    uint32_t raw[kWords + 1];
+#pragma unroll
+    for (int j = 0; j <= kWords; ++j) raw[j] = q[j];
+#pragma unroll
+    for (int j = 0; j < kWords; ++j) w[j] = __funnelshift_r(raw[j], raw[j + 1], s);
+}
+
+// Cells of a point from its coordinate words (3 floats or 3 x lo/hi of
+// doubles), exactly as (int64)fmin((p - min) / t, G - 1) in binary64.
+// Returns false when the point lies below the bounding box.
+template <bool kF32>
+__device__ __forceinline__ bool point_cells(const uint32_t* w, const CloudGrid& g, const uint8_t* smem,
+                                            const ChunkSmem& L, int cell[3]) {
+    const uint32_t G = g.grid;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        int i;
+        if (kF32) {
+            const int32_t* K = reinterpret_cast<const int32_t*>(smem + L.keys_off) + a * (G + 2);
+            const uint32_t b = w[a];
+            i = table_cell<int32_t>(dev_key32(b), __fmaf_rn(__uint_as_float(b), g.r[a], g.c[a]), K, G);
+            if (i == -2) i = exact_axis_cell((double)__uint_as_float(b), g.ax[a].mn, g.ax[a].t, G);
+        } else {
+            const long long* K = reinterpret_cast<const long long*>(smem + L.keys_off) + a * (G + 2);
+            const uint32_t lo = w[2 * a], hi = w[2 * a + 1];
+            i = table_cell<long long>(dev_key64(lo, hi), __fmaf_rn(approx_f64(lo, hi), g.r[a], g.c[a]), K, G);
+            if (i == -2) i = exact_axis_cell(__hiloint2double((int)hi, (int)lo), g.ax[a].mn, g.ax[a].t, G);
+        }
+        cell[a] = i;
+    }
+    return (cell[0] | cell[1] | cell[2]) >= 0;
+}
+
+__device__ __forceinline__ uint32_t cell_morton(const int cell[3], const uint8_t* smem, const ChunkSmem& L) {
+    const uint32_t* sp = reinterpret_cast<const uint32_t*>(smem + L.spread_off);
+    return (sp[cell[0]] << 2) | (sp[cell[1]] << 1) | sp[cell[2]];
+}
+
+// K1 (point_counting.cuh:29-53): points per finest cell.  Consecutive lanes
+// in the same cell add their count with one atomic.
+template <bool kF32>
+__global__ void __launch_bounds__(kCountThreads) k_count(const uint8_t* __restrict__ cloud, uint64_t n, uint32_t stride,
+                                                         CloudGrid g, uint32_t* __restrict__ pyr0, uint32_t* err) {
+    extern __shared__ __align__(128) uint8_t smem[];
+    const ChunkSmem L = chunk_smem(stride, g.grid, kF32, kCountTile, 0);
+    load_tables<kF32>(g, smem, L);
+    const uint32_t lane = threadIdx.x & 31;
+    tile_loop<kCountTile>(cloud, n, stride, smem, L, err, [&](const uint8_t* recs, uint64_t p0, uint32_t cnt) {
+#pragma unroll 1
+        for (uint32_t base = 0; base < kCountTile; base += kCountThreads) {
+            const uint32_t k = base + threadIdx.x;
+            uint32_t m = kNoKey;
+            if (k < cnt) {
+                constexpr int kWords = kF32 ? 3 : 6;
+                uint32_t w[kWords];
+                record_words<kWords>(recs + (uint64_t)k * stride, w);
+                int cell[3];
+                if (point_cells<kF32>(w, g, smem, L, cell)) m = cell_morton(cell, smem, L);
+                else set_error(err, kErrBelowBox);
+            }
+            const uint32_t starts = run_starts(m);
+            if (m != kNoKey && ((starts >> lane) & 1u)) atomicAdd(&pyr0[m], run_end(starts) - lane);
+        }
+    });
 }
 
 // Level l -> levels l+1 and l+2: one thread per level-(l+2) cell reads its 64
@@ -257,69 +376,171 @@ __global__ void k_tag_leaves(uint32_t* pyr, const uint64_t* __restrict__ loff, c
     pyr[loff[level[node]] + key[node]] = kLeafTag | node;
 }
 
-template <bool kF32>
-__global__ void __launch_bounds__(kTileThreads) k_distribute(const uint8_t* __restrict__ cloud, uint64_t n,
-                                                             uint32_t stride, CloudGrid g, OutParams op,
-                                                             const uint32_t* __restrict__ pyr,
-                                                             const uint64_t* __restrict__ loff, uint32_t depth,
-                                                             const uint64_t* __restrict__ data_idx, uint32_t* fill,
-                                                             uint32_t* __restrict__ lut, uint8_t* __restrict__ rec,
-                                                             uint32_t* err) {
-    extern __shared__ uint4 smem[];
-    const uint8_t* buf = reinterpret_cast<const uint8_t*>(smem);
+// Writes the leaf tag of every occupied finest cell into the cell: one
+// thread per level-1 cell reads its 8 children and, when some of them are
+// occupied and untagged, the nearest tagged ancestor.
+__global__ void k_push_tags(uint32_t* __restrict__ pyr, const uint64_t* __restrict__ loff, uint32_t depth, uint64_t n1,
+                            uint32_t* err) {
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i >= n1) return;
+    uint4* c = reinterpret_cast<uint4*>(pyr + i * 8);
+    uint4 a = c[0], b = c[1];
+    uint32_t v[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+    bool need = false;
+#pragma unroll
+    for (int s = 0; s < 8; ++s) need |= v[s] != 0 && !(v[s] & kLeafTag);
+    if (!need) return;
+    uint32_t tag = 0;
+    uint64_t k = i;
+    for (uint32_t l = 1; l <= depth; ++l, k >>= 3) {
+        const uint32_t w = pyr[loff[l] + k];
+        if (w & kLeafTag) {
+            tag = w;
+            break;
+        }
+    }
+    if (!tag) {
+        set_error(err, kErrTag);
+        return;
+    }
+#pragma unroll
+    for (int s = 0; s < 8; ++s)
+        if (v[s] != 0 && !(v[s] & kLeafTag)) v[s] = tag;
+    c[0] = make_uint4(v[0], v[1], v[2], v[3]);
+    c[1] = make_uint4(v[4], v[5], v[6], v[7]);
+}
+
+// Stores the 18-byte records held by lanes [r0, r0 + len) into consecutive
+// output slots starting at dst (2-byte aligned).  The run's byte image is
+// assembled in the warp's staging area with dst's 4-byte phase (five aligned
+// shared stores per lane), then copied out with coalesced 4-byte stores and a
+// 2-byte store at each ragged end.  Lane j holds its record as n = {x, y, z,
+// r | g << 16, b}.  All 32 lanes call with the same arguments.
+__device__ __forceinline__ void store_run(uint8_t* dst, uint32_t r0, uint32_t len, const uint32_t (&n)[5],
+                                          uint8_t* stage) {
     const uint32_t lane = threadIdx.x & 31;
-    for (uint64_t tile = blockIdx.x; tile * kTilePoints < n; tile += gridDim.x) {
-        uint64_t p0 = tile * kTilePoints;
-        uint32_t cnt = (uint32_t)((n - p0) < (uint64_t)kTilePoints ? (n - p0) : (uint64_t)kTilePoints);
-        uint32_t shift = stage_tile(cloud, p0, cnt, stride, smem);
-        __syncthreads();
-        for (uint32_t base = 0; base < cnt; base += blockDim.x) {
-            uint32_t k = base + threadIdx.x;
-            bool valid = k < cnt;
-            Coord c[3];
-            uint32_t col[3];
-            uint32_t node = 0;
-            if (valid) {
-                bool below;
-                uint32_t m = point_cell<kF32>(buf + shift + (uint64_t)k * stride, g, c, col, below);
-                if (below) {
-                    set_error(err, kErrBelowBox);
-                    valid = false;
+    const uint32_t h = (uint32_t)reinterpret_cast<uintptr_t>(dst) & 2u;   // bytes before dst in its word
+    if (lane >= r0 && lane < r0 + len) {
+        const uint32_t off = h + 18 * (lane - r0);
+        const bool al = (off & 2u) == 0;
+        // aligned record: words x, y, z, r|g at off, b at off + 16;
+        // otherwise x's low half at off, then the record shifted by 16 bits
+        const uint32_t o16 = al ? off + 16 : off;
+        const uint32_t o32 = al ? off : off + 2;
+        *reinterpret_cast<uint16_t*>(stage + o16) = (uint16_t)(al ? n[4] : n[0]);
+        uint32_t* q = reinterpret_cast<uint32_t*>(stage + o32);
+        q[0] = al ? n[0] : __funnelshift_r(n[0], n[1], 16);
+        q[1] = al ? n[1] : __funnelshift_r(n[1], n[2], 16);
+        q[2] = al ? n[2] : __funnelshift_r(n[2], n[3], 16);
+        q[3] = al ? n[3] : __funnelshift_r(n[3], n[4], 16);
+    }
+    __syncwarp();
+    const uint32_t bytes = h + 18 * len;
+    uint32_t* gw = reinterpret_cast<uint32_t*>(dst - h);
+    const uint32_t* sw = reinterpret_cast<const uint32_t*>(stage);
+    if (h && lane == 0) *reinterpret_cast<uint16_t*>(dst) = *reinterpret_cast<const uint16_t*>(stage + 2);
+    if ((bytes & 2u) && lane == 1)
+        *reinterpret_cast<uint16_t*>(dst - h + bytes - 2) = *reinterpret_cast<const uint16_t*>(stage + bytes - 2);
+    for (uint32_t w = (h >> 1) + lane; w < (bytes >> 2); w += 32) gw[w] = sw[w];
+    __syncwarp();
+}
+
+// K5 (point_distributing.cuh:30-75): every point goes to its leaf's bucket
+// with its LUT entry and 18-byte output record.  The first lane of each run
+// of equal cells reads the cell's leaf tag; the first lane of each run of
+// equal leaves reserves the run's slots with one atomic.
+template <bool kF32>
+__global__ void __launch_bounds__(kDistThreads) k_distribute(const uint8_t* __restrict__ cloud, uint64_t n,
+                                                              uint32_t stride, CloudGrid g, OutParams op,
+                                                              const uint32_t* __restrict__ pyr0,
+                                                              const uint64_t* __restrict__ data_idx, uint32_t* fill,
+                                                              uint32_t* __restrict__ lut, uint8_t* __restrict__ rec,
+                                                              uint32_t* err) {
+    extern __shared__ __align__(128) uint8_t smem[];
+    const ChunkSmem L = chunk_smem(stride, g.grid, kF32, kDistTile, (kDistThreads / 32) * kStageBytes);
+    load_tables<kF32>(g, smem, L);
+    const uint32_t lane = threadIdx.x & 31;
+    uint8_t* stage = smem + L.stage_off + (threadIdx.x >> 5) * kStageBytes;
+    tile_loop<kDistTile>(cloud, n, stride, smem, L, err, [&](const uint8_t* recs, uint64_t p0, uint32_t cnt) {
+#pragma unroll 1
+        for (uint32_t base = 0; base < kDistTile; base += kDistThreads) {
+            const uint32_t k = base + threadIdx.x;
+            constexpr int kWords = kF32 ? 4 : 7;
+            uint32_t w[kWords];
+            uint32_t m = kNoKey;
+            if (k < cnt) {
+                record_words<kWords>(recs + (uint64_t)k * stride, w);
+                int cell[3];
+                if (point_cells<kF32>(w, g, smem, L, cell)) m = cell_morton(cell, smem, L);
+                else set_error(err, kErrBelowBox);
+            }
+            uint32_t starts = run_starts(m);
+            uint32_t leader = run_leader(starts);
+            uint32_t tag = (m != kNoKey && lane == leader) ? pyr0[m] : 0u;
+            tag = __shfl_sync(0xffffffffu, tag, leader);
+            uint32_t node = kNoKey;
+            if (m != kNoKey) {
+                if (tag & kLeafTag) node = tag & ~kLeafTag;
+                else set_error(err, kErrTag);
+            }
+            starts = run_starts(node);
+            leader = run_leader(starts);
+            uint64_t first = 0;
+            if (node != kNoKey && lane == leader) first = data_idx[node] + atomicAdd(&fill[node], run_end(starts) - lane);
+            first = ((uint64_t)__shfl_sync(0xffffffffu, (uint32_t)(first >> 32), leader) << 32) |
+                    __shfl_sync(0xffffffffu, (uint32_t)first, leader);
+            uint32_t nw[5] = {0, 0, 0, 0, 0};
+            bool ok = false;
+            if (node != kNoKey) {
+                const uint64_t pos = first + (lane - leader);
+                if (pos >= n) {   // only reachable with corrupted input tags
+                    set_error(err, kErrCapacity);
                 } else {
-                    uint32_t v = pyr[m];
-                    uint32_t l = 0;
-                    while (!(v & kLeafTag)) {
-                        if (++l > depth) break;
-                        m >>= 3;
-                        v = pyr[loff[l] + m];
-                    }
-                    if (!(v & kLeafTag)) {
-                        set_error(err, kErrTag);
-                        valid = false;
+                    ok = true;
+                    lut[pos] = (uint32_t)(p0 + k);
+                    Coord c[3];
+                    uint32_t col;
+                    if (kF32) {
+                        for (int a = 0; a < 3; ++a) c[a] = coord_f32(__uint_as_float(w[a]));
+                        col = w[3];
                     } else {
-                        node = v & ~kLeafTag;
+                        for (int a = 0; a < 3; ++a)
+                            c[a] = coord_f64(__hiloint2double((int)w[2 * a + 1], (int)w[2 * a]));
+                        col = w[6];
                     }
+                    const int32_t x = out_coord<kF32>(c[0], op.ax[0]);
+                    const int32_t y = out_coord<kF32>(c[1], op.ax[1]);
+                    const int32_t z = out_coord<kF32>(c[2], op.ax[2]);
+                    if (x == kCoordError || y == kCoordError || z == kCoordError) set_error(err, kErrCoordRange);
+                    nw[0] = (uint32_t)x;
+                    nw[1] = (uint32_t)y;
+                    nw[2] = (uint32_t)z;
+                    nw[3] = (col & 0xFFu) | (((col >> 8) & 0xFFu) << 16);
+                    nw[4] = (col >> 16) & 0xFFu;
                 }
             }
-            unsigned active = __ballot_sync(0xffffffffu, valid);
-            if (valid) {
-                unsigned peers = __match_any_sync(active, node);
-                int leader = __ffs(peers) - 1;
-                uint32_t slot0 = 0;
-                if ((int)lane == leader) slot0 = atomicAdd(&fill[node], (uint32_t)__popc(peers));
-                slot0 = __shfl_sync(peers, slot0, leader);
-                uint32_t slot = slot0 + __popc(peers & ((1u << lane) - 1));
-                uint64_t pos = data_idx[node] + slot;
-                lut[pos] = (uint32_t)(p0 + k);
-                int32_t x = out_coord<kF32>(c[0], op.ax[0]);
-                int32_t y = out_coord<kF32>(c[1], op.ax[1]);
-                int32_t z = out_coord<kF32>(c[2], op.ax[2]);
-                if (x == kCoordError || y == kCoordError || z == kCoordError) set_error(err, kErrCoordRange);
-                store_record(rec, pos, x, y, z, (uint16_t)col[0], (uint16_t)col[1], (uint16_t)col[2]);
+            // records: each run of lanes bound for one leaf fills a contiguous
+            // range; warps with many runs store per lane
+            const uint32_t okmask = __ballot_sync(0xffffffffu, ok);
+            uint32_t runs = starts & okmask;
+            if (__popc(runs) <= 4) {
+                while (runs) {
+                    const uint32_t r0 = __ffs(runs) - 1;
+                    runs &= runs - 1;
+                    const uint32_t above = starts & ~(0xffffffffu >> (31 - r0));
+                    const uint32_t len = (above ? (uint32_t)__ffs(above) - 1 : 32u) - r0;
+                    const uint64_t f = ((uint64_t)__shfl_sync(0xffffffffu, (uint32_t)(first >> 32), r0) << 32) |
+                                       __shfl_sync(0xffffffffu, (uint32_t)first, r0);
+                    if (f + len <= n && ((okmask >> r0) & ((len == 32) ? 0xffffffffu : ((1u << len) - 1))) ==
+                                            ((len == 32) ? 0xffffffffu : ((1u << len) - 1)))
+                        store_run(rec + f * 18, r0, len, nw, stage);
+                }
+            } else if (ok) {
+                store_record(rec, first + (lane - leader), (int32_t)nw[0], (int32_t)nw[1], (int32_t)nw[2],
+                             (uint16_t)(nw[3] & 0xFFFFu), (uint16_t)(nw[3] >> 16), (uint16_t)nw[4]);
             }
         }
-        __syncthreads();
-    }
+    });
 }
 
 // Copies byte range [src, src + bytes) to dst.  Both addresses are even (18-byte
@@ -379,22 +600,26 @@ __global__ void k_place_lut(const uint64_t* __restrict__ src_off, const uint64_t
 
 }   // namespace
 
-static size_t tile_smem(uint32_t stride) {
-    return (size_t)kTilePoints * stride + 64;
+template <class Kernel>
+static int chunk_grid_size(Kernel kernel, uint32_t threads, uint32_t tile, size_t smem, uint64_t n, int num_sms) {
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    const uint64_t tiles = (n + tile - 1) / tile;
+    return (int)std::min<uint64_t>(tiles, (uint64_t)num_sms * per_sm);
 }
 
 int launch_count(const uint8_t* cloud, uint64_t n, uint32_t stride, bool float_input, const CloudGrid& g,
                   uint32_t* pyr0, uint32_t* err, int num_sms, cudaStream_t stream) {
-    size_t smem = tile_smem(stride);
-    uint64_t tiles = (n + kTilePoints - 1) / kTilePoints;
-    int grid = (int)std::min<uint64_t>(tiles, (uint64_t)num_sms * 4);
-    if (grid == 0) return 0;
+    if (n == 0) return 0;
+    const size_t smem = chunk_smem(stride, g.grid, float_input, kCountTile, 0).total;
     if (float_input) {
-        cudaFuncSetAttribute(k_count<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_count<true><<<grid, kTileThreads, smem, stream>>>(cloud, n, stride, g, pyr0, err);
+        const int grid = chunk_grid_size(k_count<true>, kCountThreads, kCountTile, smem, n, num_sms);
+        k_count<true><<<grid, kCountThreads, smem, stream>>>(cloud, n, stride, g, pyr0, err);
     } else {
-        cudaFuncSetAttribute(k_count<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_count<false><<<grid, kTileThreads, smem, stream>>>(cloud, n, stride, g, pyr0, err);
+        const int grid = chunk_grid_size(k_count<false>, kCountThreads, kCountTile, smem, n, num_sms);
+        k_count<false><<<grid, kCountThreads, smem, stream>>>(cloud, n, stride, g, pyr0, err);
     }
     return 1;
 }
@@ -441,22 +666,27 @@ int launch_tag_leaves(uint32_t* pyr, const uint64_t* loff_dev, const uint32_t* l
     return 1;
 }
 
+int launch_push_tags(uint32_t* pyr, const uint64_t* loff_dev, uint32_t depth, uint32_t grid, uint32_t* err,
+                     cudaStream_t stream) {
+    const uint64_t n1 = (uint64_t)(grid / 2) * (grid / 2) * (grid / 2);
+    if (!n1) return 0;
+    k_push_tags<<<(unsigned)((n1 + 255) / 256), 256, 0, stream>>>(pyr, loff_dev, depth, n1, err);
+    return 1;
+}
+
 int launch_distribute(const uint8_t* cloud, uint64_t n, uint32_t stride, bool float_input, const CloudGrid& g,
-                       const OutParams& out, const uint32_t* pyr, const uint64_t* loff_dev, uint32_t depth,
-                       const uint64_t* data_idx, uint32_t* fill, uint32_t* lut, uint8_t* rec, uint32_t* err,
-                       int num_sms, cudaStream_t stream) {
-    size_t smem = tile_smem(stride);
-    uint64_t tiles = (n + kTilePoints - 1) / kTilePoints;
-    int grid = (int)std::min<uint64_t>(tiles, (uint64_t)num_sms * 4);
-    if (grid == 0) return 0;
+                      const OutParams& out, const uint32_t* pyr0, const uint64_t* data_idx, uint32_t* fill,
+                      uint32_t* lut, uint8_t* rec, uint32_t* err, int num_sms, cudaStream_t stream) {
+    if (n == 0) return 0;
+    const size_t smem = chunk_smem(stride, g.grid, float_input, kDistTile, (kDistThreads / 32) * kStageBytes).total;
     if (float_input) {
-        cudaFuncSetAttribute(k_distribute<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_distribute<true><<<grid, kTileThreads, smem, stream>>>(cloud, n, stride, g, out, pyr, loff_dev, depth,
-                                                                 data_idx, fill, lut, rec, err);
+        const int grid = chunk_grid_size(k_distribute<true>, kDistThreads, kDistTile, smem, n, num_sms);
+        k_distribute<true><<<grid, kDistThreads, smem, stream>>>(cloud, n, stride, g, out, pyr0, data_idx, fill, lut,
+                                                                  rec, err);
     } else {
-        cudaFuncSetAttribute(k_distribute<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_distribute<false><<<grid, kTileThreads, smem, stream>>>(cloud, n, stride, g, out, pyr, loff_dev, depth,
-                                                                  data_idx, fill, lut, rec, err);
+        const int grid = chunk_grid_size(k_distribute<false>, kDistThreads, kDistTile, smem, n, num_sms);
+        k_distribute<false><<<grid, kDistThreads, smem, stream>>>(cloud, n, stride, g, out, pyr0, data_idx, fill,
+                                                                   lut, rec, err);
     }
     return 1;
 }

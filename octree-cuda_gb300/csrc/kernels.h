@@ -12,11 +12,24 @@
 
 namespace oc {
 
-// Gridding of the finest chunking level (mapPointToGrid parameters).
+// Gridding of the finest chunking level (mapPointToGrid parameters).  The
+// cell of a coordinate is looked up in exact boundary-key tables (built on the
+// host by make_cell_keys) around an fp32 estimate p * r + c; `ax` is the
+// binary64 fallback.
 struct CloudGrid {
     AxisGrid ax[3];
-    uint32_t grid;   // chunking grid G0
+    float r[3];               // float(1 / t)
+    float c[3];               // float(-min / t)
+    uint32_t grid;            // chunking grid G0
+    const void* keys;         // device: 3 x (grid + 2) keys, int64 (double input) or int32 (float input)
+    const uint32_t* spread;   // device: spread3(i) for i < grid
 };
+
+// Exact boundary keys of one axis for the reference's cell formula
+// (int64)fmin((p - mn) / t, grid - 1): keys[i] = least ordered key of a
+// coordinate whose cell is >= i, keys[grid] = keys[grid + 1] = largest key.
+void make_cell_keys64(double mn, double t, uint32_t grid, int64_t* keys);
+void make_cell_keys32(double mn, double t, uint32_t grid, int32_t* keys);
 
 // Output-coordinate parameters: cloud bbox minimum and 1/scale per axis.
 struct OutParams {
@@ -119,10 +132,14 @@ int launch_enumerate(const uint32_t* pyr, const uint64_t* level_off_dev, uint32_
 int launch_tag_leaves(uint32_t* pyr, const uint64_t* level_off_dev, const uint32_t* leaf_nodes, uint32_t n_leaves,
                        const uint32_t* key, const uint8_t* level, cudaStream_t stream);
 
+// Writes each occupied finest-level cell's leaf tag into the cell (after
+// launch_tag_leaves), so that distribution finds a point's leaf in one read.
+int launch_push_tags(uint32_t* pyr, const uint64_t* level_off_dev, uint32_t depth, uint32_t grid, uint32_t* err,
+                     cudaStream_t stream);
+
 int launch_distribute(const uint8_t* cloud, uint64_t n, uint32_t stride, bool float_input, const CloudGrid& g,
-                       const OutParams& out, const uint32_t* pyr, const uint64_t* level_off_dev, uint32_t depth,
-                       const uint64_t* data_idx, uint32_t* fill, uint32_t* lut, uint8_t* rec, uint32_t* err,
-                       int num_sms, cudaStream_t stream);
+                      const OutParams& out, const uint32_t* pyr0, const uint64_t* data_idx, uint32_t* fill,
+                      uint32_t* lut, uint8_t* rec, uint32_t* err, int num_sms, cudaStream_t stream);
 
 size_t subsample_smem_bytes();
 uint32_t subsample_block_size();

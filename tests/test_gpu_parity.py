@@ -148,3 +148,18 @@ def test_repeat_generate_same_session():
     r2, l2 = node_sorted(s.hierarchy(), s.records(), s.lut())
     assert np.array_equal(l1, l2) and r1.tobytes() == r2.tobytes()
     s.close()
+
+
+@pytest.mark.parametrize("cloud_type", [0, 1])
+def test_shuffled_point_order(cloud_type):
+    """Points in random order: warps see many cells and leaves at once, so the
+    per-point paths of counting and distribution (no runs of equal keys) are
+    exercised."""
+    from helpers import Case
+
+    case = make_case(1, cloud_type, 300_000, seed=33)
+    perm = np.random.default_rng(5).permutation(case.n)
+    recs = case.cloud[: case.n * case.stride].reshape(case.n, case.stride)[perm].reshape(-1)
+    case = Case(np.ascontiguousarray(recs), case.n, case.stride, case.cloud_type, case.scale, case.bb_min, case.bb_max)
+    cfg = dict(chunk_grid=128, sub_grid=64, merge_threshold=3000, inter=True)
+    compare_results(run_oracle(case, cfg), run_gpu(case, cfg))
