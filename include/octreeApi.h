@@ -151,7 +151,8 @@ OCPI_EXPORT int ocpi_get_timings(void* session, double* ms, int max, char* names
  *                     (used by random subsampling)
  *   modeFlags         OCPI_SUB_* bits, as ocpi_configure_subsampling selects
  *   candidateLut      device: cloud index of every candidate point
- *   candidateRecords  device: the candidates' 18-byte octree.bin records
+ *   candidateRecords  device: the candidates' 18-byte octree.bin records,
+ *                     readable for 16 bytes past the last record
  *   outLut, outRecords device: room for candidateCount entries / records
  *   outStatus         device, 2 words: [0] points written, [1] error bits
  *                     (1 point below the node box, 4 brick table overflow)

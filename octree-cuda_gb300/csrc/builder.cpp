@@ -173,7 +173,7 @@ Builder::Builder(const BuildConfig& cfg, const uint8_t* host_cloud, int device) 
     }
     cloud_.ensure((size_t)cfg_.n * cfg_.stride + 64);
     lut_.ensure((size_t)cfg_.n * 4);
-    rec_.ensure((size_t)cfg_.n * 18);
+    rec_.ensure((size_t)cfg_.n * 18 + 16);   // 16 readable bytes past the last record
     upload(host_cloud);
 }
 
@@ -372,88 +372,127 @@ void Builder::subsample() {
     const bool inter = !intra && cfg_.inter;
     const bool weighted = inter && cfg_.weighting;
     const bool averaged = intra || inter;
-    stage_used_ = 0;
-    stats_.p_in = 0;
     OutParams op;
     for (int a = 0; a < 3; ++a) op.ax[a] = make_out_axis(cfg_.bb_min[a], 1.0 / cfg_.scale[a]);
 
+    // ---- static part of the node tables, all levels.  Upper bounds of the
+    // points per node: out(v) <= min(sum over children, S^3).
+    const uint64_t S3 = (uint64_t)S * S * S;
+    const size_t n = nodes_.size();
+    std::vector<uint64_t> out_bound(n, 0), in_bound(n, 0);
+    for (size_t i = n; i-- > 0;) {
+        const NodeHost& v = nodes_[i];
+        if (!v.internal) {
+            out_bound[i] = v.points;
+            continue;
+        }
+        uint64_t b = 0;
+        uint32_t c = v.child_first;
+        for (uint32_t s = 0; s < 8; ++s)
+            if (v.mask & (1u << s)) b += out_bound[c++];
+        in_bound[i] = b;
+        out_bound[i] = std::min(b, S3);
+    }
+    // per level, largest bound first (the persistent blocks take nodes in this
+    // order); internal index = position in the level-major order
+    std::vector<uint32_t> level_first(depth_ + 2, 0), ii_of(n, 0xFFFFFFFFu);
+    std::vector<uint32_t> order;
+    uint64_t max_level_bound = 0, max_node_bound = 0;
     for (uint32_t l = 1; l <= depth_; ++l) {
-        auto& list = internal_by_level_[l];
-        if (list.empty()) continue;
-        // largest nodes first: the persistent blocks take them in this order
-        auto p_in_of = [&](uint32_t vi) {
-            const NodeHost& v = nodes_[vi];
-            uint64_t p = 0;
-            uint32_t c = v.child_first;
-            for (uint32_t s = 0; s < 8; ++s)
-                if (v.mask & (1u << s)) p += nodes_[c++].points;
-            return p;
-        };
-        std::vector<std::pair<uint64_t, uint32_t>> order;
-        for (uint32_t vi : list) order.push_back({p_in_of(vi), vi});
-        std::stable_sort(order.begin(), order.end(),
-                         [](const auto& x, const auto& y) { return x.first > y.first; });
-        for (size_t k = 0; k < list.size(); ++k) list[k] = order[k].second;
-        const double side = cubic / std::pow(2.0, (double)(depth_ - l));   // fp_subsampling.cu:16-17
-        const double t = side / S;                                         // kernel_helpers.cuh:14
-        std::vector<SubNode> table(list.size());
-        uint64_t level_in = 0, max_p_in = 0;
-        for (size_t k = 0; k < list.size(); ++k) {
-            const NodeHost& v = nodes_[list[k]];
-            SubNode& sn = table[k];
-            std::memset(&sn, 0, sizeof(sn));
-            for (int a = 0; a < 3; ++a) {
-                sn.ax[a] = make_axis(v.mn[a], t);
-                sn.qa[a] = make_qaxis(v.mn[a], cfg_.bb_min[a], 1.0 / cfg_.scale[a], t);
-            }
-            sn.morton = v.key;
-            sn.level = l;
-            uint32_t c = v.child_first, nc = 0;
-            uint64_t p = 0;
-            for (uint32_t s = 0; s < 8; ++s) {
-                if (!(v.mask & (1u << s))) continue;
-                const NodeHost& ch = nodes_[c++];
-                if (ch.internal) {
-                    sn.child_kind |= 1u << nc;
-                    sn.child_start[nc] = ch.stage_off;
-                } else {
-                    sn.child_start[nc] = ch.data_idx;
-                }
+        auto list = internal_by_level_[l];
+        std::stable_sort(list.begin(), list.end(),
+                         [&](uint32_t x, uint32_t y) { return in_bound[x] > in_bound[y]; });
+        level_first[l] = (uint32_t)order.size();
+        uint64_t lb = 0;
+        for (uint32_t vi : list) {
+            ii_of[vi] = (uint32_t)order.size();
+            order.push_back(vi);
+            lb += in_bound[vi];
+            max_node_bound = std::max(max_node_bound, in_bound[vi]);
+        }
+        max_level_bound = std::max(max_level_bound, lb);
+    }
+    level_first[depth_ + 1] = (uint32_t)order.size();
+    const uint32_t n_internal = (uint32_t)order.size();
+    std::vector<SubNode> table(n_internal);
+    for (uint32_t k = 0; k < n_internal; ++k) {
+        const NodeHost& v = nodes_[order[k]];
+        SubNode& sn = table[k];
+        std::memset(&sn, 0, sizeof(sn));
+        const double side = cubic / std::pow(2.0, (double)(depth_ - v.level));   // fp_subsampling.cu:16-17
+        const double t = side / S;                                               // kernel_helpers.cuh:14
+        for (int a = 0; a < 3; ++a) {
+            sn.ax[a] = make_axis(v.mn[a], t);
+            sn.qa[a] = make_qaxis(v.mn[a], cfg_.bb_min[a], 1.0 / cfg_.scale[a], t);
+        }
+        sn.morton = v.key;
+        sn.level = v.level;
+        uint32_t c = v.child_first, nc = 0;
+        for (uint32_t s = 0; s < 8; ++s) {
+            if (!(v.mask & (1u << s))) continue;
+            const uint32_t ci = c++;
+            const NodeHost& ch = nodes_[ci];
+            if (ch.internal) {
+                sn.child_kind |= 1u << nc;
+                sn.child_start[nc] = ii_of[ci];   // replaced on the device by the staged position
+            } else {
+                sn.child_start[nc] = ch.data_idx;
                 sn.child_count[nc] = ch.points;
-                p += ch.points;
-                ++nc;
             }
-            sn.nchild = nc;
-            if (p > 0xFFFFFFFFull) throw Error("internal node too large");
-            sn.p_in = (uint32_t)p;
-            sn.cand_off = level_in;
-            max_p_in = std::max<uint64_t>(max_p_in, p);
-            level_in += p;
+            ++nc;
         }
-        stats_.p_in += level_in;
-        // scratch and staging capacity
-        key_cache_.ensure(level_in * 4);
-        acc_best_.ensure(level_in * 8);
-        cell_slot_.ensure(level_in * 4);
-        if (cfg_.random) acc_sel_.ensure(level_in * 4);
-        if (averaged && !weighted) acc_intra_.ensure(level_in * 8);
+        sn.nchild = nc;
+    }
+
+    // ---- capacities: the staging arrays hold every level's candidates
+    // (N + P_out at most, bounded by the reference's output capacity) and the
+    // scratch one level's; both grow and the pass is repeated if a level does
+    // not fit
+    const uint64_t out_cap = (uint64_t)((float)cfg_.n * cfg_.output_factor);   // octree_processor_impl.cu:24-31
+    uint64_t stage_cap = std::max<uint64_t>(sub_stage_cap_, std::max<uint64_t>(out_cap, cfg_.n));
+    uint64_t scratch_cap = std::max<uint64_t>(sub_scratch_cap_, std::min(max_level_bound, stage_cap));
+    {
+        // global brick tables: enough slots for the largest node at 68% load
+        // (bricks <= candidates and <= bricks of the grid)
+        const uint64_t bs = (S + 3) / 4;
+        const uint64_t bound = std::min<uint64_t>(max_node_bound, bs * bs * bs);
+        uint64_t cap = 1024;
+        while (cap * 11 / 16 < bound + 1) cap <<= 1;
+        uint32_t shift = 32;
+        for (uint64_t c = cap; c > 1; c >>= 1) --shift;
+        size_t max_level_nodes = 0;
+        for (uint32_t l = 1; l <= depth_; ++l)
+            max_level_nodes = std::max<size_t>(max_level_nodes, level_first[l + 1] - level_first[l]);
+        const size_t blocks = std::min<size_t>(max_level_nodes, (size_t)num_sms_);
+        g_key_.ensure(blocks * cap * 4);
+        g_mask_.ensure(blocks * cap * 8);
+        g_base_.ensure(blocks * cap * 4);
+        g_cap_ = (uint32_t)cap;
+        g_shift_ = shift;
+    }
+    out_points_.ensure((size_t)n_internal * 4 + 4);
+    stage_off_.ensure((size_t)n_internal * 8 + 8);
+    level_base_.ensure(8);
+    work_.ensure(4);
+
+    for (int attempt = 0;; ++attempt) {
+        key_cache_.ensure(scratch_cap * 4);
+        acc_best_.ensure(scratch_cap * 8);
+        cell_slot_.ensure(scratch_cap * 4);
+        if (cfg_.random) acc_sel_.ensure(scratch_cap * 4);
+        if (averaged && !weighted) acc_intra_.ensure(scratch_cap * 8);
         if (weighted) {
-            unit_cache_.ensure(level_in * 12);
-            csr_count_.ensure(level_in * 4);
-            csr_start_.ensure(level_in * 4);
-            csr_pts_.ensure(level_in * 20);
+            unit_cache_.ensure(scratch_cap * 12);
+            csr_count_.ensure(scratch_cap * 4);
+            csr_start_.ensure(scratch_cap * 4);
+            csr_pts_.ensure(scratch_cap * 20);
         }
-        uint64_t need = stage_used_ + level_in;
-        stage_lut_.ensure_keep(need * 4, stage_used_ * 4, stream_);
-        stage_rec_.ensure_keep(need * 18 + 64, stage_used_ * 18, stream_);
+        stage_lut_.ensure(stage_cap * 4);
+        stage_rec_.ensure(stage_cap * 18 + 64);
         upload_vec(sub_nodes_, table, stream_);
-        out_points_.ensure(list.size() * 4);
-        work_.ensure(4);
-        check_cuda(cudaMemsetAsync(work_.p, 0, 4, stream_), "memset");
+        check_cuda(cudaMemsetAsync(level_base_.p, 0, 8, stream_), "memset");
 
         SubLevelArgs a{};
-        a.nodes = sub_nodes_.as<SubNode>();
-        a.n_nodes = (uint32_t)list.size();
         a.grid = S;
         a.mode = mode;
         a.float_input = cfg_.cloud_type == 0;
@@ -464,9 +503,8 @@ void Builder::subsample() {
         a.leaf_rec = rec_.as<uint8_t>();
         a.stage_lut = stage_lut_.as<uint32_t>();
         a.stage_rec = stage_rec_.as<uint8_t>();
-        a.out_lut = stage_lut_.as<uint32_t>() + stage_used_;
-        a.out_rec = stage_rec_.as<uint8_t>() + stage_used_ * 18;
-        a.out_points = out_points_.as<uint32_t>();
+        a.out_lut = stage_lut_.as<uint32_t>();
+        a.out_rec = stage_rec_.as<uint8_t>();
         a.key_cache = key_cache_.as<uint32_t>();
         a.unit_cache = unit_cache_.as<float>();
         a.acc_best = acc_best_.as<uint64_t>();
@@ -479,41 +517,55 @@ void Builder::subsample() {
         a.out = op;
         a.work_counter = work_.as<uint32_t>();
         a.err = err_.as<uint32_t>();
-        {
-            // global brick tables: enough slots for the level's largest node
-            // at 68% load (bricks <= candidates and <= bricks of the grid)
-            uint64_t bs = (S + 3) / 4;
-            uint64_t bound = std::min<uint64_t>(max_p_in, bs * bs * bs);
-            uint64_t cap = 1024;
-            while (cap * 11 / 16 < bound + 1) cap <<= 1;
-            uint32_t shift = 32;
-            for (uint64_t c = cap; c > 1; c >>= 1) --shift;
-            size_t blocks = (size_t)std::min<uint64_t>(list.size(), (uint64_t)num_sms_);
-            g_key_.ensure(blocks * cap * 4);
-            g_mask_.ensure(blocks * cap * 8);
-            g_base_.ensure(blocks * cap * 4);
-            a.global_key = g_key_.as<uint32_t>();
-            a.global_mask = g_mask_.as<uint64_t>();
-            a.global_base = g_base_.as<uint32_t>();
-            a.global_cap = (uint32_t)cap;
-            a.global_shift = shift;
+        a.global_key = g_key_.as<uint32_t>();
+        a.global_mask = g_mask_.as<uint64_t>();
+        a.global_base = g_base_.as<uint32_t>();
+        a.global_cap = g_cap_;
+        a.global_shift = g_shift_;
+        for (uint32_t l = 1; l <= depth_; ++l) {
+            const uint32_t first = level_first[l], cnt = level_first[l + 1] - first;
+            if (!cnt) continue;
+            SubNode* lvl = sub_nodes_.as<SubNode>() + first;
+            launches_ += launch_prepare_level(lvl, cnt, out_points_.as<uint32_t>(), stage_off_.as<uint64_t>(), first,
+                                              level_base_.as<uint64_t>(), scratch_cap, stage_cap,
+                                              work_.as<uint32_t>(), err_.as<uint32_t>(), stream_);
+            a.nodes = lvl;
+            a.n_nodes = cnt;
+            a.out_points = out_points_.as<uint32_t>() + first;
+            launches_ += launch_subsample_level(a, num_sms_, stream_);
+            char mark[32];
+            std::snprintf(mark, sizeof mark, "sub_l%u", l);
+            stage_mark(mark);
         }
-        char mark[32];
-        std::snprintf(mark, sizeof mark, "sub_host_l%u", l);
-        stage_mark(mark);
-        launches_ += launch_subsample_level(a, num_sms_, stream_);
-        std::snprintf(mark, sizeof mark, "sub_l%u", l);
-        stage_mark(mark);
         check_cuda(cudaGetLastError(), "subsample launch");
-        std::vector<uint32_t> pts(list.size());
-        check_cuda(cudaMemcpyAsync(pts.data(), out_points_.p, pts.size() * 4, cudaMemcpyDeviceToHost, stream_), "D2H");
-        check_cuda(cudaStreamSynchronize(stream_), "subsample level");
-        for (size_t k = 0; k < list.size(); ++k) {
-            NodeHost& v = nodes_[list[k]];
-            v.points = pts[k];
-            v.stage_off = stage_used_ + table[k].cand_off;
+        uint32_t e = 0;
+        uint64_t used = 0;
+        check_cuda(cudaMemcpyAsync(&e, err_.p, 4, cudaMemcpyDeviceToHost, stream_), "D2H err");
+        check_cuda(cudaMemcpyAsync(&used, level_base_.p, 8, cudaMemcpyDeviceToHost, stream_), "D2H");
+        check_cuda(cudaStreamSynchronize(stream_), "subsample");
+        if (!(e & kErrCapacity)) {
+            stage_used_ = used;
+            break;
         }
-        stage_used_ += level_in;
+        if (attempt >= 6 || (e & ~kErrCapacity)) check_device_errors("subsample");
+        // a level did not fit: grow and repeat the pass
+        stage_cap *= 2;
+        scratch_cap = std::min<uint64_t>(scratch_cap * 2, std::max(max_level_bound, scratch_cap));
+        const uint32_t keep = e & ~kErrCapacity;
+        check_cuda(cudaMemcpyAsync(err_.p, &keep, 4, cudaMemcpyHostToDevice, stream_), "H2D err");
+    }
+    sub_stage_cap_ = stage_cap;
+    sub_scratch_cap_ = scratch_cap;
+    stats_.p_in = stage_used_;
+
+    std::vector<uint32_t> pts(n_internal);
+    std::vector<uint64_t> soff(n_internal);
+    check_cuda(cudaMemcpy(pts.data(), out_points_.p, (size_t)n_internal * 4, cudaMemcpyDeviceToHost), "D2H");
+    check_cuda(cudaMemcpy(soff.data(), stage_off_.p, (size_t)n_internal * 8, cudaMemcpyDeviceToHost), "D2H");
+    for (uint32_t k = 0; k < n_internal; ++k) {
+        NodeHost& v = nodes_[order[k]];
+        v.points = pts[k];
+        v.stage_off = soff[k];
     }
 }
 
@@ -547,7 +599,7 @@ void Builder::place_internal() {
     p_out_ = off - cfg_.n;
     uint64_t total = off;
     lut_.ensure_keep(total * 4, (size_t)cfg_.n * 4, stream_);
-    rec_.ensure_keep(total * 18, (size_t)cfg_.n * 18, stream_);
+    rec_.ensure_keep(total * 18 + 16, (size_t)cfg_.n * 18, stream_);
     upload_vec(place_src_, src, stream_);
     upload_vec(place_dst_, dst, stream_);
     upload_vec(place_cnt_, cnt, stream_);

@@ -131,6 +131,9 @@ private:
     DevBuf place_src_, place_dst_, place_cnt_;
     DevBuf g_key_, g_mask_, g_base_;   // per-block global brick tables
     DevBuf cell_keys_, spread_;         // chunking-grid boundary keys and Morton spread table
+    DevBuf stage_off_, level_base_;     // staged position of each internal node's outputs; staging fill
+    uint64_t sub_stage_cap_ = 0, sub_scratch_cap_ = 0;   // capacities that fit the last build
+    uint32_t g_cap_ = 0, g_shift_ = 0;
     uint32_t launches_ = 0;
     size_t place_count_ = 0;
     bool lut_placed_ = false;

@@ -525,6 +525,46 @@ __device__ __forceinline__ uint32_t run_end(uint32_t starts) {
     return higher ? (uint32_t)__ffs(higher) - 1 : 32u;
 }
 
+// ---------------------------------------------------------------------------
+// Warp-cooperative output of consecutive 18-byte records.
+
+constexpr uint32_t kStageBytes = 592;   // per-warp staging area: >= 2 + 32 * 18 + 2, 16-byte multiple
+
+// Stores the 18-byte records held by lanes [r0, r0 + len) into consecutive
+// output slots starting at dst (2-byte aligned).  The run's byte image is
+// assembled in the warp's staging area with dst's 4-byte phase (five aligned
+// shared stores per lane), then copied out with coalesced 4-byte stores and a
+// 2-byte store at each ragged end.  Lane j holds its record as n = {x, y, z,
+// r | g << 16, b}.  All 32 lanes call with the same arguments.
+__device__ __forceinline__ void store_run(uint8_t* dst, uint32_t r0, uint32_t len, const uint32_t (&n)[5],
+                                          uint8_t* stage) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t h = (uint32_t)reinterpret_cast<uintptr_t>(dst) & 2u;   // bytes before dst in its word
+    if (lane >= r0 && lane < r0 + len) {
+        const uint32_t off = h + 18 * (lane - r0);
+        const bool al = (off & 2u) == 0;
+        // aligned record: words x, y, z, r|g at off, b at off + 16;
+        // otherwise x's low half at off, then the record shifted by 16 bits
+        const uint32_t o16 = al ? off + 16 : off;
+        const uint32_t o32 = al ? off : off + 2;
+        *reinterpret_cast<uint16_t*>(stage + o16) = (uint16_t)(al ? n[4] : n[0]);
+        uint32_t* q = reinterpret_cast<uint32_t*>(stage + o32);
+        q[0] = al ? n[0] : __funnelshift_r(n[0], n[1], 16);
+        q[1] = al ? n[1] : __funnelshift_r(n[1], n[2], 16);
+        q[2] = al ? n[2] : __funnelshift_r(n[2], n[3], 16);
+        q[3] = al ? n[3] : __funnelshift_r(n[3], n[4], 16);
+    }
+    __syncwarp();
+    const uint32_t bytes = h + 18 * len;
+    uint32_t* gw = reinterpret_cast<uint32_t*>(dst - h);
+    const uint32_t* sw = reinterpret_cast<const uint32_t*>(stage);
+    if (h && lane == 0) *reinterpret_cast<uint16_t*>(dst) = *reinterpret_cast<const uint16_t*>(stage + 2);
+    if ((bytes & 2u) && lane == 1)
+        *reinterpret_cast<uint16_t*>(dst - h + bytes - 2) = *reinterpret_cast<const uint16_t*>(stage + bytes - 2);
+    for (uint32_t w = (h >> 1) + lane; w < (bytes >> 2); w += 32) gw[w] = sw[w];
+    __syncwarp();
+}
+
 #endif   // __CUDACC__
 
 }   // namespace oc

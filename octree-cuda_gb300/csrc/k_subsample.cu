@@ -244,6 +244,8 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
     __shared__ uint32_t warp_sums[32];
     __shared__ uint32_t s_bricks, s_overflow;
     BrickMap sm_map;
+    // per-warp staging area of the emitted records, after the brick table
+    uint8_t* stage = reinterpret_cast<uint8_t*>(dyn + 2 * kBrickSlots) + (threadIdx.x >> 5) * kStageBytes;
     sm_map.mask = dyn;
     sm_map.key = reinterpret_cast<uint32_t*>(dyn + kBrickSlots);
     sm_map.base = sm_map.key + kBrickSlots;
@@ -286,6 +288,7 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
         const AxisGrid ax0 = nd.ax[0], ax1 = nd.ax[1], ax2 = nd.ax[2];
         const QAxis qa0 = nd.qa[0], qa1 = nd.qa[1], qa2 = nd.qa[2];
         const uint64_t off = nd.cand_off;
+        const uint64_t oo = nd.out_off;
         const uint32_t level = nd.level;
         const uint64_t morton = nd.morton;
         BrickMap bm = sm_map;
@@ -488,64 +491,150 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
             __syncthreads();
         }
 
-        // ---- emit one record per occupied cell (thread per cell, rank order)
-        for (uint32_t r = threadIdx.x; r < cells; r += blockDim.x) {
-            const uint32_t ks = a.cell_slot[off + r];
-            const uint32_t slot = ks >> 6, bit = ks & 63;
-            const uint32_t brick = bm.key[slot] - 1;
-            const int bx = (int)(brick & 0xFF), by = (int)((brick >> 8) & 0xFF), bz = (int)(brick >> 16);
-            const int lx = (int)(bit & 3), ly = (int)((bit >> 2) & 3), lz = (int)((bit >> 4) & 3);
-            const uint64_t best = a.acc_best[off + r];
-            const uint32_t idx = random ? (uint32_t)best : (uint32_t)(best >> 32);
-            const uint32_t jsel = random ? a.acc_sel[off + r] : (uint32_t)best;
-            // the winner's record holds its output coordinates (same cloud
-            // minimum and scale at every level) and, unaveraged, its colour
-            uint32_t csel = 0;
-            while (csel + 1 < ns.nchild && ns.prefix[csel + 1] <= jsel) ++csel;
-            const uint64_t spos = ns.start[csel] + (jsel - ns.prefix[csel]);
-            const uint16_t* srec =
-                reinterpret_cast<const uint16_t*>((((ns.kind >> csel) & 1u) ? a.stage_rec : a.leaf_rec) + spos * 18);
-            uint16_t rw[9];
-#pragma unroll
-            for (int q = 0; q < 9; ++q) rw[q] = srec[q];
-            uint16_t cr = rw[6], cg = rw[7], cb = rw[8];
-            if (intra) {
-                decode_colors(a.acc_intra[off + r], cr, cg, cb);
-            } else if (inter && !weighted) {
-                InterSum f{a.acc_intra + off, 0};
-                visit_neighbours(bm, slot, bx, by, bz, lx, ly, lz, f);
-                decode_colors(f.e, cr, cg, cb);
-            } else if (weighted) {
-                WeightedSum f{a.csr_start + off, a.csr_count + off, a.csr_pts + off * 20,
-                              bx * 4 + lx, by * 4 + ly, bz * 4 + lz, 0, 0, 0, 0};
-                visit_neighbours(bm, slot, bx, by, bz, lx, ly, lz, f);
-                if (f.sw) {
-                    cr = (uint16_t)(f.sr / f.sw);
-                    cg = (uint16_t)(f.sg / f.sw);
-                    cb = (uint16_t)(f.sb / f.sw);
+        // ---- emit one record per occupied cell (thread per cell, rank order;
+        // each warp writes 32 consecutive records with coalesced stores)
+        for (uint32_t r0 = threadIdx.x & ~31u; r0 < cells; r0 += blockDim.x) {
+            const uint32_t r = r0 + (threadIdx.x & 31);
+            uint32_t nw[5] = {0, 0, 0, 0, 0};
+            if (r < cells) {
+                const uint32_t ks = a.cell_slot[off + r];
+                const uint32_t slot = ks >> 6, bit = ks & 63;
+                const uint32_t brick = bm.key[slot] - 1;
+                const int bx = (int)(brick & 0xFF), by = (int)((brick >> 8) & 0xFF), bz = (int)(brick >> 16);
+                const int lx = (int)(bit & 3), ly = (int)((bit >> 2) & 3), lz = (int)((bit >> 4) & 3);
+                const uint64_t best = a.acc_best[off + r];
+                const uint32_t idx = random ? (uint32_t)best : (uint32_t)(best >> 32);
+                const uint32_t jsel = random ? a.acc_sel[off + r] : (uint32_t)best;
+                // the winner's record holds its output coordinates (same cloud
+                // minimum and scale at every level) and, unaveraged, its colour
+                uint32_t csel = 0;
+                while (csel + 1 < ns.nchild && ns.prefix[csel + 1] <= jsel) ++csel;
+                const uint64_t spos = ns.start[csel] + (jsel - ns.prefix[csel]);
+                const uintptr_t sa =
+                    reinterpret_cast<uintptr_t>((((ns.kind >> csel) & 1u) ? a.stage_rec : a.leaf_rec) + spos * 18);
+                // 20 bytes from the 4-byte boundary below the record (the record
+                // arrays keep 16 readable bytes past their end)
+                const uint32_t* sq = reinterpret_cast<const uint32_t*>(sa & ~(uintptr_t)3);
+                const uint32_t sh = (uint32_t)(sa & 2) * 8;
+                const uint32_t q0 = sq[0], q1 = sq[1], q2 = sq[2], q3 = sq[3], q4 = sq[4];
+                nw[0] = __funnelshift_r(q0, q1, sh);
+                nw[1] = __funnelshift_r(q1, q2, sh);
+                nw[2] = __funnelshift_r(q2, q3, sh);
+                const uint32_t w3 = __funnelshift_r(q3, q4, sh);
+                uint16_t cr = (uint16_t)w3, cg = (uint16_t)(w3 >> 16), cb = (uint16_t)(q4 >> sh);
+                if (intra) {
+                    decode_colors(a.acc_intra[off + r], cr, cg, cb);
+                } else if (inter && !weighted) {
+                    InterSum f{a.acc_intra + off, 0};
+                    visit_neighbours(bm, slot, bx, by, bz, lx, ly, lz, f);
+                    decode_colors(f.e, cr, cg, cb);
+                } else if (weighted) {
+                    WeightedSum f{a.csr_start + off, a.csr_count + off, a.csr_pts + off * 20,
+                                  bx * 4 + lx, by * 4 + ly, bz * 4 + lz, 0, 0, 0, 0};
+                    visit_neighbours(bm, slot, bx, by, bz, lx, ly, lz, f);
+                    if (f.sw) {
+                        cr = (uint16_t)(f.sr / f.sw);
+                        cg = (uint16_t)(f.sg / f.sw);
+                        cb = (uint16_t)(f.sb / f.sw);
+                    }
                 }
+                a.out_lut[oo + r] = idx;
+                nw[3] = (uint32_t)cr | ((uint32_t)cg << 16);
+                nw[4] = cb;
             }
-            a.out_lut[off + r] = idx;
-            uint16_t* dst = reinterpret_cast<uint16_t*>(a.out_rec + (off + r) * 18);
-#pragma unroll
-            for (int q = 0; q < 6; ++q) dst[q] = rw[q];
-            dst[6] = cr;
-            dst[7] = cg;
-            dst[8] = cb;
+            store_run(a.out_rec + (oo + r0) * 18, 0, min(32u, cells - r0), nw, stage);
         }
         if (threadIdx.x == 0) a.out_points[ni] = cells;
         __syncthreads();
     }
 }
 
+__device__ __forceinline__ uint64_t block_exclusive_scan64(uint64_t v, uint64_t* warp_sums, uint64_t& total) {
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint64_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint64_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= (uint32_t)o) x += y;
+    }
+    if (lane == 31) warp_sums[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint64_t w = lane < (blockDim.x >> 5) ? warp_sums[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint64_t y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= (uint32_t)o) w += y;
+        }
+        warp_sums[lane] = w;
+    }
+    __syncthreads();
+    const uint64_t warp_prefix = warp ? warp_sums[warp - 1] : 0;
+    total = warp_sums[(blockDim.x >> 5) - 1];
+    __syncthreads();
+    return warp_prefix + x - v;
+}
+
+__global__ void __launch_bounds__(1024) k_prepare_level(SubNode* nodes, uint32_t n_nodes, const uint32_t* out_points,
+                                                        uint64_t* stage_off, uint32_t first_internal,
+                                                        uint64_t* level_base, uint64_t scratch_cap,
+                                                        uint64_t stage_cap, uint32_t* work_counter, uint32_t* err) {
+    __shared__ uint64_t warp_sums[32];
+    __shared__ uint32_t s_skip;
+    if (threadIdx.x == 0) s_skip = (*err & kErrCapacity) != 0;   // an earlier level overflowed
+    __syncthreads();
+    const uint64_t base = *level_base;
+    uint64_t running = 0;
+    for (uint32_t k0 = 0; k0 < n_nodes; k0 += blockDim.x) {
+        const uint32_t k = k0 + threadIdx.x;
+        uint64_t p = 0;
+        if (k < n_nodes && !s_skip) {
+            SubNode& nd = nodes[k];
+            for (uint32_t c = 0; c < nd.nchild; ++c) {
+                if ((nd.child_kind >> c) & 1u) {
+                    const uint32_t ii = (uint32_t)nd.child_start[c];
+                    nd.child_count[c] = out_points[ii];
+                    nd.child_start[c] = stage_off[ii];
+                }
+                p += nd.child_count[c];
+            }
+        }
+        uint64_t total;
+        const uint64_t pre = block_exclusive_scan64(p, warp_sums, total);
+        if (k < n_nodes && !s_skip) {
+            SubNode& nd = nodes[k];
+            nd.p_in = (uint32_t)p;
+            nd.cand_off = running + pre;
+            nd.out_off = base + running + pre;
+            stage_off[first_internal + k] = base + running + pre;
+            if (p > 0xFFFFFFFFull) atomicOr(err, kErrCapacity);
+        }
+        running += total;
+    }
+    if (threadIdx.x == 0) {
+        const bool over = s_skip || running > scratch_cap || base + running > stage_cap || (*err & kErrCapacity);
+        if (over) atomicOr(err, kErrCapacity);
+        *work_counter = over ? n_nodes : 0u;
+        *level_base = base + running;
+    }
+}
+
 }   // namespace
+
+int launch_prepare_level(SubNode* nodes, uint32_t n_nodes, const uint32_t* out_points, uint64_t* stage_off,
+                         uint32_t first_internal, uint64_t* level_base, uint64_t scratch_cap, uint64_t stage_cap,
+                         uint32_t* work_counter, uint32_t* err, cudaStream_t stream) {
+    k_prepare_level<<<1, 1024, 0, stream>>>(nodes, n_nodes, out_points, stage_off, first_internal, level_base,
+                                            scratch_cap, stage_cap, work_counter, err);
+    return 1;
+}
 
 uint32_t subsample_block_size() {
     return kSubThreads;
 }
 
 size_t subsample_smem_bytes() {
-    return (size_t)kBrickSlots * (8 + 4 + 4);
+    return (size_t)kBrickSlots * (8 + 4 + 4) + (size_t)(kSubThreads / 32) * kStageBytes;
 }
 
 namespace {

@@ -64,6 +64,7 @@ struct SubNode {
     QAxis qa[3];
     uint64_t morton;
     uint64_t cand_off;   // first candidate slot of this node in the level scratch
+    uint64_t out_off;    // first output slot of this node in out_lut / out_rec
     uint64_t child_start[8];
     uint32_t child_count[8];
     uint32_t level;
@@ -140,6 +141,18 @@ int launch_push_tags(uint32_t* pyr, const uint64_t* level_off_dev, uint32_t dept
 int launch_distribute(const uint8_t* cloud, uint64_t n, uint32_t stride, bool float_input, const CloudGrid& g,
                       const OutParams& out, const uint32_t* pyr0, const uint64_t* data_idx, uint32_t* fill,
                       uint32_t* lut, uint8_t* rec, uint32_t* err, int num_sms, cudaStream_t stream);
+
+// Fills the dynamic part of one level's node table before it is subsampled:
+// for children that are internal nodes (child_kind bit set, child_start = the
+// child's internal index on entry) their output count and staged position,
+// then p_in, cand_off (level-local) and out_off = *level_base + cand_off.
+// Records each node's out_off in stage_off[first_internal + k], advances
+// *level_base, and sets *work_counter to n_nodes (every block exits at once)
+// when the level exceeds scratch_cap or the staging arrays exceed stage_cap
+// (error kErrCapacity), else to 0.
+int launch_prepare_level(SubNode* nodes, uint32_t n_nodes, const uint32_t* out_points, uint64_t* stage_off,
+                         uint32_t first_internal, uint64_t* level_base, uint64_t scratch_cap, uint64_t stage_cap,
+                         uint32_t* work_counter, uint32_t* err, cudaStream_t stream);
 
 size_t subsample_smem_bytes();
 uint32_t subsample_block_size();

@@ -148,6 +148,7 @@ extern "C" int ocpi_subsample_node_noalloc(const uint8_t* cloud, uint8_t cloudTy
         node.morton = mortonKey;
         node.level = level;
         node.cand_off = 0;
+        node.out_off = 0;
         node.nchild = candidateCount ? 1 : 0;   // the candidates form one leaf-kind list
         node.child_kind = 0;
         node.child_start[0] = 0;

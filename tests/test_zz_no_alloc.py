@@ -68,7 +68,8 @@ def run_noalloc(torch, case, cfg, flags, sess, hier, level, key, mn, children, i
     cand_lut = np.concatenate([lut[a:b] for a, b in parts]).astype(np.uint32)
     n = len(cand_lut)
     assert 0 < n <= octree_api.NOALLOC_MAX_CANDIDATES
-    d_rec = torch.from_numpy(np.ascontiguousarray(cand_rec).reshape(-1)).cuda()
+    # 16 readable bytes past the last candidate record
+    d_rec = torch.from_numpy(np.concatenate([np.ascontiguousarray(cand_rec).reshape(-1), np.zeros(16, np.uint8)])).cuda()
     d_lut = torch.from_numpy(cand_lut.view(np.int32)).cuda()
     o_rec = torch.full((n * 18,), 0xAB, dtype=torch.uint8, device="cuda")
     o_lut = torch.full((n,), -1, dtype=torch.int32, device="cuda")
