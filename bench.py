@@ -122,6 +122,13 @@ def stage_bytes(st, n, stride, timings):
     }
 
 
+def pinned_bytes(nbytes):
+    """uint8 numpy view of page-locked host memory."""
+    import torch
+
+    return torch.empty(nbytes, dtype=torch.uint8, pin_memory=True).numpy()
+
+
 def make_cloud(n, threads):
     import octree_api
 
@@ -205,8 +212,14 @@ def main():
         if pg:
             pg.barrier()
 
+    # the cloud lives in pinned host memory (the upload in ocpi_init_octree is
+    # a DMA from it) and results are read back into pinned memory
+    cloud_host = pinned_bytes(cloud.nbytes)
+    cloud_host[:] = cloud
+    del cloud
     s = octree_api.OctreeSession(device)
-    s.set_cloud(cloud, n=n, stride=STRIDE, cloud_type=CLOUD_TYPE, scale=[SCALE] * 3, bb_min=bb[:3], bb_max=bb[3:])
+    s.set_cloud(cloud_host, n=n, stride=STRIDE, cloud_type=CLOUD_TYPE, scale=[SCALE] * 3, bb_min=bb[:3],
+                bb_max=bb[3:])
     s.configure(**CFG)
     s.init()
     for _ in range(args.warmup):
@@ -243,7 +256,7 @@ def main():
     e2e_times = []
     hier_bytes = st["tree_nodes"] * 22
     rec_bytes = st["points_total"] * 18
-    recs = np.empty(st["points_total"] * 18, np.uint8)
+    recs = pinned_bytes(st["points_total"] * 18)
     L = octree_api.load_library()
     for i in range(max(2, min(args.steps, 3))):
         barrier()
@@ -277,10 +290,12 @@ def main():
     achieved = sb[dom] / (stage_ms[dom] * 1e-3) / 1e9
     traffic = None
     try:
+        # DRAM bytes per point of the stage, from one ncu capture of this
+        # workload (profiles/dram_traffic_lod_build_120M_f64.md), scaled to n
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
-            tr = json.load(f).get(dom)
+            tr = json.load(f)["stages"].get(dom)
             if tr:
-                traffic = tr["bytes_per_point"] * n
+                traffic = int(tr["bytes_per_point"] * n)
     except Exception:
         pass
     total_alg = sum(sb.values())
@@ -305,7 +320,7 @@ def main():
     }
     if rank == 0 and not args.no_cpu_baseline:
         sample = min(CPU_SAMPLE, n)
-        t = cpu_oracle_time(cloud, bb, sample, threads)
+        t = cpu_oracle_time(cloud_host, bb, sample, threads)
         line["cpu_baseline"] = {"value": round(sample / t / 1e6, 3), "unit": "Mpts/s", "cores": threads,
                                 "kind": "port",
                                 "sample": "first %d points of the same cloud, same bbox and settings" % sample}
