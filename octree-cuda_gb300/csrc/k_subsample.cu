@@ -211,6 +211,60 @@ __device__ __forceinline__ void visit_neighbours(const BrickMap& bm, uint32_t sl
     }
 }
 
+// Packed colour sum over the occupied cells of the 3x3x3 neighbourhood of
+// the cell at brick-local (lx, ly, lz) of brick (bx, by, bz) held in `slot`
+// (the cell itself included).  Every lane evaluates all 27 positions with the
+// same instruction stream (selects and predicated loads instead of loops over
+// occupied neighbours), so a warp does not diverge on neighbourhood shape.
+__device__ __forceinline__ uint64_t inter_sum(const BrickMap& bm, uint32_t slot, int bx, int by, int bz, int lx,
+                                              int ly, int lz, const uint64_t* __restrict__ acc) {
+    const int sx = lx == 0 ? -1 : (lx == 3 ? 1 : 0);
+    const int sy = ly == 0 ? -1 : (ly == 3 ? 1 : 0);
+    const int sz = lz == 0 ? -1 : (lz == 3 ? 1 : 0);
+    auto find = [&](int dx, int dy, int dz) -> int {
+        const int nx = bx + dx, ny = by + dy, nz = bz + dz;
+        if (nx < 0 || ny < 0 || nz < 0 || nx >= (int)bm.bs || ny >= (int)bm.bs || nz >= (int)bm.bs) return -1;
+        return brick_find(bm, ((uint32_t)nx | ((uint32_t)ny << 8) | ((uint32_t)nz << 16)) + 1);
+    };
+    // the (up to) eight bricks: index bit 0 = x side, 1 = y side, 2 = z side
+    int sl[8];
+    sl[0] = (int)slot;
+    sl[1] = sx ? find(sx, 0, 0) : -1;
+    sl[2] = sy ? find(0, sy, 0) : -1;
+    sl[3] = (sx && sy) ? find(sx, sy, 0) : -1;
+    sl[4] = sz ? find(0, 0, sz) : -1;
+    sl[5] = (sx && sz) ? find(sx, 0, sz) : -1;
+    sl[6] = (sy && sz) ? find(0, sy, sz) : -1;
+    sl[7] = (sx && sy && sz) ? find(sx, sy, sz) : -1;
+    uint64_t e = 0;
+#pragma unroll
+    for (int dz = -1; dz <= 1; ++dz) {
+#pragma unroll
+        for (int dy = -1; dy <= 1; ++dy) {
+            const int yy = ly + dy, zz = lz + dz;
+            // leaving the brick along y or z means the cell sits on that face,
+            // so the side brick is the one looked up above
+            const int ib = (((unsigned)yy > 3u) ? 2 : 0) | (((unsigned)zz > 3u) ? 4 : 0);
+            const int so = sl[ib], ss = sl[ib | 1];
+            const uint64_t mo = so >= 0 ? bm.mask[so] : 0ull;
+            const uint32_t bo = so >= 0 ? bm.base[so] : 0u;
+            const uint64_t ms = ss >= 0 ? bm.mask[ss] : 0ull;
+            const uint32_t bsd = ss >= 0 ? bm.base[ss] : 0u;
+            const uint32_t row = (uint32_t)((yy & 3) * 4 + (zz & 3) * 16);
+#pragma unroll
+            for (int dx = -1; dx <= 1; ++dx) {
+                const int xx = lx + dx;
+                const bool side = (unsigned)xx > 3u;
+                const uint64_t m = side ? ms : mo;
+                const uint32_t bit = row + (uint32_t)(xx & 3);
+                const uint32_t rank = (side ? bsd : bo) + (uint32_t)__popcll(m & ((1ull << bit) - 1ull));
+                if ((m >> bit) & 1ull) e += __ldcg(acc + rank);   // written by this block's atomics (L2)
+            }
+        }
+    }
+    return e;
+}
+
 struct InterSum {
     const uint64_t* acc;
     uint64_t e;
@@ -525,9 +579,7 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
                 if (intra) {
                     decode_colors(a.acc_intra[off + r], cr, cg, cb);
                 } else if (inter && !weighted) {
-                    InterSum f{a.acc_intra + off, 0};
-                    visit_neighbours(bm, slot, bx, by, bz, lx, ly, lz, f);
-                    decode_colors(f.e, cr, cg, cb);
+                    decode_colors(inter_sum(bm, slot, bx, by, bz, lx, ly, lz, a.acc_intra + off), cr, cg, cb);
                 } else if (weighted) {
                     WeightedSum f{a.csr_start + off, a.csr_count + off, a.csr_pts + off * 20,
                                   bx * 4 + lx, by * 4 + ly, bz * 4 + lz, 0, 0, 0, 0};
