@@ -371,8 +371,13 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
                     const uint32_t j = jbase + k;
                     // cell from the record's quantised coordinates; the cloud point
                     // is read only when a quantisation step straddles a boundary
-                    const uint16_t* rec = src_rec + (start + k) * 9;
-                    const int32_t q0 = rec_coord(rec, 0), q1 = rec_coord(rec, 1), q2 = rec_coord(rec, 2);
+                    // x, y, z of the 18-byte record (2-byte aligned) from four aligned words
+                    const uintptr_t ra = reinterpret_cast<uintptr_t>(src_rec + (start + k) * 9);
+                    const uint32_t* rw = reinterpret_cast<const uint32_t*>(ra & ~(uintptr_t)3);
+                    const uint32_t rs = (uint32_t)(ra & 2) * 8;
+                    const uint32_t w0 = rw[0], w1 = rw[1], w2 = rw[2], w3 = rw[3];
+                    const int32_t q0 = (int32_t)__funnelshift_r(w0, w1, rs), q1 = (int32_t)__funnelshift_r(w1, w2, rs),
+                                  q2 = (int32_t)__funnelshift_r(w2, w3, rs);
                     int ix = quant_cell(q0, qa0, a.grid);
                     int iy = quant_cell(q1, qa1, a.grid);
                     int iz = quant_cell(q2, qa2, a.grid);
@@ -401,7 +406,8 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
                         s_overflow = 1;
                         break;
                     }
-                    atomicOr(reinterpret_cast<unsigned long long*>(&bm.mask[slot]), 1ull << bit);
+                    // 32-bit atomic on the half of the mask that holds the bit
+                    atomicOr(reinterpret_cast<uint32_t*>(&bm.mask[slot]) + (bit >> 5), 1u << (bit & 31));
                     a.key_cache[off + j] = (slot << 6) | bit;
                     if (weighted) {
                         a.unit_cache[(off + j) * 3 + 0] = quant_units(q0, qa0);
@@ -480,8 +486,14 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
                 else key = ((uint64_t)idx << 32) | (jbase + k);
                 atomicMin(reinterpret_cast<unsigned long long*>(&a.acc_best[off + rank]), (unsigned long long)key);
                 if (averaged && !weighted) {
-                    const uint16_t* src = reinterpret_cast<const uint16_t*>(src_rec + (start + k) * 18);
-                    const uint64_t enc = encode_colors(src[6], src[7], src[8]);
+                    // r, g, b (bytes 12..17 of the record) from two aligned words
+                    const uintptr_t ca = reinterpret_cast<uintptr_t>(src_rec + (start + k) * 18 + 12);
+                    const uint32_t* cw = reinterpret_cast<const uint32_t*>(ca & ~(uintptr_t)3);
+                    const uint32_t cs = (uint32_t)(ca & 2) * 8;
+                    const uint32_t c0 = cw[0], c1 = cw[1];
+                    const uint32_t rg = __funnelshift_r(c0, c1, cs);
+                    const uint32_t bb = (c1 >> cs) & 0xFFFFu;
+                    const uint64_t enc = encode_colors(rg & 0xFFFFu, rg >> 16, bb);
                     atomicAdd(reinterpret_cast<unsigned long long*>(&a.acc_intra[off + rank]), (unsigned long long)enc);
                 }
                 if (weighted) atomicAdd(&a.csr_count[off + rank], 1u);
