@@ -302,10 +302,7 @@ void Builder::generate() {
     stage_mark("distribute");
     check_cuda(cudaGetLastError(), "launch");
 
-    subsample();
-    stage_mark("subsample");
-    place_internal();
-    stage_mark("place");
+    subsample();   // also places the internal nodes' records (stage marks "sub_l*", "place")
     check_cuda(cudaGetLastError(), "launch");
     check_device_errors("generate");
     collect_timings();
@@ -414,6 +411,30 @@ void Builder::subsample() {
     }
     level_first[depth_ + 1] = (uint32_t)order.size();
     const uint32_t n_internal = (uint32_t)order.size();
+    // DFS post-order of the internal nodes (calculateWritingPosition,
+    // kernel_helpers.cuh:55-59; setActiveParent fp_subsampling.cu:183): their
+    // records follow the N leaf points in this order
+    std::vector<uint32_t> post;
+    post.reserve(n_internal);
+    {
+        std::vector<std::pair<uint32_t, bool>> st{{0u, false}};
+        uint32_t kids[8];
+        while (!st.empty()) {
+            const auto [i, expanded] = st.back();
+            st.pop_back();
+            const NodeHost& v = nodes_[i];
+            if (!v.internal) continue;
+            if (expanded) {
+                post.push_back(ii_of[i]);
+                continue;
+            }
+            st.push_back({i, true});
+            uint32_t nk = 0, c = v.child_first;
+            for (uint32_t s = 0; s < 8; ++s)
+                if (v.mask & (1u << s)) kids[nk++] = c++;
+            while (nk) st.push_back({kids[--nk], false});
+        }
+    }
     std::vector<SubNode> table(n_internal);
     for (uint32_t k = 0; k < n_internal; ++k) {
         const NodeHost& v = nodes_[order[k]];
@@ -470,6 +491,14 @@ void Builder::subsample() {
         g_cap_ = (uint32_t)cap;
         g_shift_ = shift;
     }
+    // final record arrays: N leaf records (written) + P_out internal records
+    uint64_t rec_cap = std::max<uint64_t>(sub_rec_cap_, std::max<uint64_t>(out_cap, cfg_.n));
+    upload_vec(post_ii_, post, stream_);
+    place_src_.ensure((size_t)n_internal * 8 + 8);
+    place_dst_.ensure((size_t)n_internal * 8 + 8);
+    place_cnt_.ensure((size_t)n_internal * 4 + 4);
+    node_dst_.ensure((size_t)n_internal * 8 + 8);
+    out_total_.ensure(8);
     out_points_.ensure((size_t)n_internal * 4 + 4);
     stage_off_.ensure((size_t)n_internal * 8 + 8);
     level_base_.ensure(8);
@@ -489,6 +518,8 @@ void Builder::subsample() {
         }
         stage_lut_.ensure(stage_cap * 4);
         stage_rec_.ensure(stage_cap * 18 + 64);
+        lut_.ensure_keep(rec_cap * 4, (size_t)cfg_.n * 4, stream_);
+        rec_.ensure_keep(rec_cap * 18 + 16, (size_t)cfg_.n * 18, stream_);
         upload_vec(sub_nodes_, table, stream_);
         check_cuda(cudaMemsetAsync(level_base_.p, 0, 8, stream_), "memset");
 
@@ -537,76 +568,52 @@ void Builder::subsample() {
             std::snprintf(mark, sizeof mark, "sub_l%u", l);
             stage_mark(mark);
         }
+        // internal nodes' records to their post-order positions
+        launches_ += launch_place_prepare(post_ii_.as<uint32_t>(), n_internal, out_points_.as<uint32_t>(),
+                                          stage_off_.as<uint64_t>(), cfg_.n, rec_cap, place_src_.as<uint64_t>(),
+                                          place_dst_.as<uint64_t>(), place_cnt_.as<uint32_t>(),
+                                          node_dst_.as<uint64_t>(), out_total_.as<uint64_t>(), err_.as<uint32_t>(),
+                                          stream_);
+        launches_ += launch_place(place_src_.as<uint64_t>(), place_dst_.as<uint64_t>(), place_cnt_.as<uint32_t>(),
+                                  n_internal, stage_rec_.as<uint8_t>(), rec_.as<uint8_t>(), stream_);
+        stage_mark("place");
         check_cuda(cudaGetLastError(), "subsample launch");
         uint32_t e = 0;
         uint64_t used = 0;
         check_cuda(cudaMemcpyAsync(&e, err_.p, 4, cudaMemcpyDeviceToHost, stream_), "D2H err");
         check_cuda(cudaMemcpyAsync(&used, level_base_.p, 8, cudaMemcpyDeviceToHost, stream_), "D2H");
+        check_cuda(cudaMemcpyAsync(&p_out_, out_total_.p, 8, cudaMemcpyDeviceToHost, stream_), "D2H");
         check_cuda(cudaStreamSynchronize(stream_), "subsample");
         if (!(e & kErrCapacity)) {
             stage_used_ = used;
             break;
         }
         if (attempt >= 6 || (e & ~kErrCapacity)) check_device_errors("subsample");
-        // a level did not fit: grow and repeat the pass
+        // a level or the final records did not fit: grow and repeat the pass
         stage_cap *= 2;
         scratch_cap = std::min<uint64_t>(scratch_cap * 2, std::max(max_level_bound, scratch_cap));
+        rec_cap = std::max<uint64_t>(rec_cap * 2, (uint64_t)cfg_.n + stage_cap);
         const uint32_t keep = e & ~kErrCapacity;
         check_cuda(cudaMemcpyAsync(err_.p, &keep, 4, cudaMemcpyHostToDevice, stream_), "H2D err");
     }
     sub_stage_cap_ = stage_cap;
     sub_scratch_cap_ = scratch_cap;
+    sub_rec_cap_ = rec_cap;
     stats_.p_in = stage_used_;
+    place_count_ = n_internal;
+    lut_placed_ = false;
 
     std::vector<uint32_t> pts(n_internal);
-    std::vector<uint64_t> soff(n_internal);
+    std::vector<uint64_t> soff(n_internal), dst(n_internal);
     check_cuda(cudaMemcpy(pts.data(), out_points_.p, (size_t)n_internal * 4, cudaMemcpyDeviceToHost), "D2H");
     check_cuda(cudaMemcpy(soff.data(), stage_off_.p, (size_t)n_internal * 8, cudaMemcpyDeviceToHost), "D2H");
+    check_cuda(cudaMemcpy(dst.data(), node_dst_.p, (size_t)n_internal * 8, cudaMemcpyDeviceToHost), "D2H");
     for (uint32_t k = 0; k < n_internal; ++k) {
         NodeHost& v = nodes_[order[k]];
         v.points = pts[k];
         v.stage_off = soff[k];
+        v.data_idx = dst[k];
     }
-}
-
-void Builder::place_internal() {
-    // DFS post-order after the N leaf points (calculateWritingPosition,
-    // kernel_helpers.cuh:55-59; setActiveParent fp_subsampling.cu:183)
-    std::vector<uint64_t> src, dst;
-    std::vector<uint32_t> cnt;
-    uint64_t off = cfg_.n;
-    std::vector<std::pair<uint32_t, bool>> st{{0u, false}};
-    while (!st.empty()) {
-        auto [i, expanded] = st.back();
-        st.pop_back();
-        NodeHost& v = nodes_[i];
-        if (!v.internal) continue;
-        if (expanded) {
-            v.data_idx = off;
-            off += v.points;
-            src.push_back(v.stage_off);
-            dst.push_back(v.data_idx);
-            cnt.push_back(v.points);
-            continue;
-        }
-        st.push_back({i, true});
-        std::vector<uint32_t> kids;
-        uint32_t c = v.child_first;
-        for (uint32_t s = 0; s < 8; ++s)
-            if (v.mask & (1u << s)) kids.push_back(c++);
-        for (auto it = kids.rbegin(); it != kids.rend(); ++it) st.push_back({*it, false});
-    }
-    p_out_ = off - cfg_.n;
-    uint64_t total = off;
-    lut_.ensure_keep(total * 4, (size_t)cfg_.n * 4, stream_);
-    rec_.ensure_keep(total * 18 + 16, (size_t)cfg_.n * 18, stream_);
-    upload_vec(place_src_, src, stream_);
-    upload_vec(place_dst_, dst, stream_);
-    upload_vec(place_cnt_, cnt, stream_);
-    place_count_ = cnt.size();
-    launches_ += launch_place(place_src_.as<uint64_t>(), place_dst_.as<uint64_t>(), place_cnt_.as<uint32_t>(),
-                              (uint32_t)cnt.size(), stage_rec_.as<uint8_t>(), rec_.as<uint8_t>(), stream_);
-    lut_placed_ = false;
 }
 
 void Builder::compute_stats() {
@@ -684,8 +691,7 @@ void Builder::copy_lut(uint32_t* out) {
     // internal-node cloud indices are moved to their final positions on demand
     if (!lut_placed_) {
         launch_place_lut(place_src_.as<uint64_t>(), place_dst_.as<uint64_t>(), place_cnt_.as<uint32_t>(),
-                         (uint32_t)(place_cnt_.bytes ? place_count_ : 0), stage_lut_.as<uint32_t>(), lut_.as<uint32_t>(),
-                         stream_);
+                         (uint32_t)place_count_, stage_lut_.as<uint32_t>(), lut_.as<uint32_t>(), stream_);
         check_cuda(cudaStreamSynchronize(stream_), "place lut");
         lut_placed_ = true;
     }

@@ -110,7 +110,6 @@ private:
     void check_device_errors(const char* stage);
     void build_tree_host(uint32_t n_nodes);
     void subsample();
-    void place_internal();
     void compute_stats();
 
     BuildConfig cfg_;
@@ -132,7 +131,8 @@ private:
     DevBuf g_key_, g_mask_, g_base_;   // per-block global brick tables
     DevBuf cell_keys_, spread_;         // chunking-grid boundary keys and Morton spread table
     DevBuf stage_off_, level_base_;     // staged position of each internal node's outputs; staging fill
-    uint64_t sub_stage_cap_ = 0, sub_scratch_cap_ = 0;   // capacities that fit the last build
+    DevBuf post_ii_, node_dst_, out_total_;   // post-order of internal nodes, their output positions, P_out
+    uint64_t sub_stage_cap_ = 0, sub_scratch_cap_ = 0, sub_rec_cap_ = 0;   // capacities that fit the last build
     uint32_t g_cap_ = 0, g_shift_ = 0;
     uint32_t launches_ = 0;
     size_t place_count_ = 0;

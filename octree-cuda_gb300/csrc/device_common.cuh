@@ -526,6 +526,36 @@ __device__ __forceinline__ uint32_t run_end(uint32_t starts) {
 }
 
 // ---------------------------------------------------------------------------
+// Block-wide exclusive scan of one 64-bit value per thread (all threads call;
+// warp_sums holds 32 entries).
+
+__device__ __forceinline__ uint64_t block_exclusive_scan64(uint64_t v, uint64_t* warp_sums, uint64_t& total) {
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint64_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint64_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= (uint32_t)o) x += y;
+    }
+    if (lane == 31) warp_sums[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint64_t w = lane < (blockDim.x >> 5) ? warp_sums[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint64_t y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= (uint32_t)o) w += y;
+        }
+        warp_sums[lane] = w;
+    }
+    __syncthreads();
+    const uint64_t warp_prefix = warp ? warp_sums[warp - 1] : 0;
+    total = warp_sums[(blockDim.x >> 5) - 1];
+    __syncthreads();
+    return warp_prefix + x - v;
+}
+
+// ---------------------------------------------------------------------------
 // Warp-cooperative output of consecutive 18-byte records.
 
 constexpr uint32_t kStageBytes = 592;   // per-warp staging area: >= 2 + 32 * 18 + 2, 16-byte multiple

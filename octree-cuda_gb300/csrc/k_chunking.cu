@@ -552,6 +552,43 @@ __global__ void k_place(const uint64_t* __restrict__ src_off, const uint64_t* __
         copy_bytes_even(rec + dst_off[v] * 18, stage_rec + src_off[v] * 18, (uint64_t)count[v] * 18);
 }
 
+// Output positions of the internal nodes: DFS post-order after the N leaf
+// points (calculateWritingPosition, kernel_helpers.cuh:55-59).  One block
+// scans the nodes' point counts in post-order (post[] lists internal indices)
+// and writes the copy list of k_place; nothing is copied when an earlier stage
+// reported a capacity error or the records exceed `cap`.
+__global__ void __launch_bounds__(1024) k_place_prepare(const uint32_t* __restrict__ post, uint32_t n_internal,
+                                                        const uint32_t* __restrict__ points,
+                                                        const uint64_t* __restrict__ stage_off, uint64_t n,
+                                                        uint64_t cap, uint64_t* src, uint64_t* dst, uint32_t* cnt,
+                                                        uint64_t* node_dst, uint64_t* total, uint32_t* err) {
+    __shared__ uint64_t warp_sums[32];
+    const bool skip = (*err & kErrCapacity) != 0;
+    uint64_t running = 0;
+    for (uint32_t k0 = 0; k0 < n_internal; k0 += blockDim.x) {
+        const uint32_t k = k0 + threadIdx.x;
+        const uint32_t ii = k < n_internal ? post[k] : 0;
+        const uint64_t p = (k < n_internal && !skip) ? points[ii] : 0;
+        uint64_t sum;
+        const uint64_t pre = block_exclusive_scan64(p, warp_sums, sum);
+        if (k < n_internal) {
+            const uint64_t d = n + running + pre;
+            src[k] = skip ? 0 : stage_off[ii];
+            dst[k] = d;
+            cnt[k] = (uint32_t)p;
+            node_dst[ii] = d;
+        }
+        running += sum;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        *total = running;
+        if (!skip && n + running > cap) atomicOr(err, kErrCapacity);
+    }
+    if (!skip && n + running > cap)   // nothing may be written past the record arrays
+        for (uint32_t k = threadIdx.x; k < n_internal; k += blockDim.x) cnt[k] = 0;
+}
+
 __global__ void k_place_lut(const uint64_t* __restrict__ src_off, const uint64_t* __restrict__ dst_off,
                             const uint32_t* __restrict__ count, uint32_t n_nodes,
                             const uint32_t* __restrict__ stage_lut, uint32_t* __restrict__ lut) {
@@ -660,6 +697,14 @@ int launch_place(const uint64_t* src_off, const uint64_t* dst_off, const uint32_
     if (!n_nodes) return 0;
     unsigned grid = n_nodes < 8192 ? n_nodes : 8192;
     k_place<<<grid, 256, 0, stream>>>(src_off, dst_off, count, n_nodes, stage_rec, rec);
+    return 1;
+}
+
+int launch_place_prepare(const uint32_t* post, uint32_t n_internal, const uint32_t* points, const uint64_t* stage_off,
+                         uint64_t n, uint64_t cap, uint64_t* src, uint64_t* dst, uint32_t* cnt, uint64_t* node_dst,
+                         uint64_t* total, uint32_t* err, cudaStream_t stream) {
+    k_place_prepare<<<1, 1024, 0, stream>>>(post, n_internal, points, stage_off, n, cap, src, dst, cnt, node_dst, total,
+                                            err);
     return 1;
 }
 

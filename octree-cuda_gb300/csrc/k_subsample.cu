@@ -613,32 +613,6 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
     }
 }
 
-__device__ __forceinline__ uint64_t block_exclusive_scan64(uint64_t v, uint64_t* warp_sums, uint64_t& total) {
-    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint64_t x = v;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint64_t y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= (uint32_t)o) x += y;
-    }
-    if (lane == 31) warp_sums[warp] = x;
-    __syncthreads();
-    if (warp == 0) {
-        uint64_t w = lane < (blockDim.x >> 5) ? warp_sums[lane] : 0;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint64_t y = __shfl_up_sync(0xffffffffu, w, o);
-            if (lane >= (uint32_t)o) w += y;
-        }
-        warp_sums[lane] = w;
-    }
-    __syncthreads();
-    const uint64_t warp_prefix = warp ? warp_sums[warp - 1] : 0;
-    total = warp_sums[(blockDim.x >> 5) - 1];
-    __syncthreads();
-    return warp_prefix + x - v;
-}
-
 __global__ void __launch_bounds__(1024) k_prepare_level(SubNode* nodes, uint32_t n_nodes, const uint32_t* out_points,
                                                         uint64_t* stage_off, uint32_t first_internal,
                                                         uint64_t* level_base, uint64_t scratch_cap,

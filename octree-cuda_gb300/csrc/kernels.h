@@ -162,6 +162,12 @@ int launch_subsample_level(const SubLevelArgs& a, int num_sms, cudaStream_t stre
 int launch_place(const uint64_t* src_off, const uint64_t* dst_off, const uint32_t* count, uint32_t n_nodes,
                  const uint8_t* stage_rec, uint8_t* rec, cudaStream_t stream);
 // Same for the per-record cloud indices.
+// Post-order output positions of the internal nodes and the copy list of
+// launch_place (see k_place_prepare).
+int launch_place_prepare(const uint32_t* post, uint32_t n_internal, const uint32_t* points, const uint64_t* stage_off,
+                         uint64_t n, uint64_t cap, uint64_t* src, uint64_t* dst, uint32_t* cnt, uint64_t* node_dst,
+                         uint64_t* total, uint32_t* err, cudaStream_t stream);
+
 int launch_place_lut(const uint64_t* src_off, const uint64_t* dst_off, const uint32_t* count, uint32_t n_nodes,
                      const uint32_t* stage_lut, uint32_t* lut, cudaStream_t stream);
 
