@@ -256,7 +256,10 @@ def main():
     e2e_times = []
     hier_bytes = st["tree_nodes"] * 22
     rec_bytes = st["points_total"] * 18
-    recs = pinned_bytes(st["points_total"] * 18)
+    # results land in pinned host arrays registered with the session: the
+    # leaf records stream back while the upper levels are subsampled
+    recs = pinned_bytes(max(int(np.float32(n) * np.float32(CFG["output_factor"])), st["points_total"]) * 18)
+    s.set_output_host(recs)
     L = octree_api.load_library()
     for i in range(max(2, min(args.steps, 3))):
         barrier()

@@ -117,6 +117,17 @@ OCPI_EXPORT int ocpi_get_level_counts(void* session, uint32_t level, uint32_t* o
  * values and their names (comma separated) into names (size name_bytes). */
 OCPI_EXPORT int ocpi_get_timings(void* session, double* ms, int max, char* names, int name_bytes, int* count);
 
+/* Registers host arrays that every later ocpi_generate_octree fills before it
+ * returns: octree.bin records (and, if lut is not NULL, the source index of
+ * each record), `capacity` records each.  The leaf records are copied while
+ * the upper levels are being subsampled, so with page-locked (pinned) arrays
+ * most of the read-back overlaps the build.  ocpi_get_records / ocpi_get_lut
+ * on the same arrays then copy nothing.  The arrays must stay valid until the
+ * next ocpi_generate_octree returns; generate fails when the octree has more
+ * than `capacity` records (outputFactor * N is always enough for builds the
+ * reference can hold).  records = NULL unregisters. */
+OCPI_EXPORT int ocpi_set_output_host(void* session, uint8_t* records, uint32_t* lut, uint64_t capacity);
+
 /* ---- allocation-free node subsampling (no counterpart in the reference) --
  *
  * For callers that may not allocate device memory: a plug-in living inside an

@@ -178,6 +178,9 @@ Builder::Builder(const BuildConfig& cfg, const uint8_t* host_cloud, int device) 
 }
 
 Builder::~Builder() {
+    if (copy_stream_) cudaStreamSynchronize(copy_stream_);
+    if (leaf_ready_) cudaEventDestroy(leaf_ready_);
+    if (copy_stream_) cudaStreamDestroy(copy_stream_);
     for (auto e : event_pool_) cudaEventDestroy(e);
     if (stream_) cudaStreamDestroy(stream_);
 }
@@ -207,6 +210,18 @@ void Builder::collect_timings() {
     }
 }
 
+void Builder::set_output_host(uint8_t* records, uint32_t* lut, uint64_t capacity) {
+    if (copy_stream_) check_cuda(cudaStreamSynchronize(copy_stream_), "output copies");
+    host_rec_ = records;
+    host_lut_ = records ? lut : nullptr;
+    host_cap_ = records ? capacity : 0;
+    host_filled_ = false;
+    if (records && !copy_stream_) {
+        check_cuda(cudaStreamCreateWithFlags(&copy_stream_, cudaStreamNonBlocking), "stream");
+        check_cuda(cudaEventCreateWithFlags(&leaf_ready_, cudaEventDisableTiming), "event");
+    }
+}
+
 void Builder::upload(const uint8_t* host_cloud) {
     if (!host_cloud) throw Error("no point cloud set");
     stage_begin();
@@ -230,6 +245,8 @@ void Builder::check_device_errors(const char* stage) {
 }
 
 void Builder::generate() {
+    host_filled_ = false;
+    if (host_rec_ && host_cap_ < cfg_.n) throw Error("output host buffer holds fewer records than the cloud");
     const double cubic = cfg_.bb_max[0] - cfg_.bb_min[0];
     CloudGrid g;
     g.grid = cfg_.chunk_grid;
@@ -518,8 +535,20 @@ void Builder::subsample() {
         }
         stage_lut_.ensure(stage_cap * 4);
         stage_rec_.ensure(stage_cap * 18 + 64);
+        if (copy_stream_) check_cuda(cudaStreamSynchronize(copy_stream_), "output copies");
         lut_.ensure_keep(rec_cap * 4, (size_t)cfg_.n * 4, stream_);
         rec_.ensure_keep(rec_cap * 18 + 16, (size_t)cfg_.n * 18, stream_);
+        if (host_rec_) {
+            // leaf records (and LUT entries) are final: stream them to the
+            // caller's arrays while the levels are subsampled
+            check_cuda(cudaEventRecord(leaf_ready_, stream_), "event");
+            check_cuda(cudaStreamWaitEvent(copy_stream_, leaf_ready_, 0), "wait");
+            check_cuda(cudaMemcpyAsync(host_rec_, rec_.p, (size_t)cfg_.n * 18, cudaMemcpyDeviceToHost, copy_stream_),
+                       "D2H records");
+            if (host_lut_)
+                check_cuda(cudaMemcpyAsync(host_lut_, lut_.p, (size_t)cfg_.n * 4, cudaMemcpyDeviceToHost, copy_stream_),
+                           "D2H lut");
+        }
         upload_vec(sub_nodes_, table, stream_);
         check_cuda(cudaMemsetAsync(level_base_.p, 0, 8, stream_), "memset");
 
@@ -613,6 +642,28 @@ void Builder::subsample() {
         v.points = pts[k];
         v.stage_off = soff[k];
         v.data_idx = dst[k];
+    }
+    if (host_rec_) {
+        const uint64_t total = (uint64_t)cfg_.n + p_out_;
+        if (total > host_cap_) {
+            check_cuda(cudaStreamSynchronize(copy_stream_), "output copies");
+            throw Error("output host buffer too small: the octree has " + std::to_string(total) + " records");
+        }
+        check_cuda(cudaMemcpyAsync(host_rec_ + (size_t)cfg_.n * 18, rec_.as<uint8_t>() + (size_t)cfg_.n * 18,
+                                   (size_t)p_out_ * 18, cudaMemcpyDeviceToHost, stream_),
+                   "D2H records");
+        if (host_lut_) {
+            launch_place_lut(place_src_.as<uint64_t>(), place_dst_.as<uint64_t>(), place_cnt_.as<uint32_t>(),
+                             (uint32_t)place_count_, stage_lut_.as<uint32_t>(), lut_.as<uint32_t>(), stream_);
+            lut_placed_ = true;
+            check_cuda(cudaMemcpyAsync(host_lut_ + cfg_.n, lut_.as<uint32_t>() + cfg_.n, (size_t)p_out_ * 4,
+                                       cudaMemcpyDeviceToHost, stream_),
+                       "D2H lut");
+        }
+        stage_mark("d2h");
+        check_cuda(cudaStreamSynchronize(copy_stream_), "output copies");
+        check_cuda(cudaStreamSynchronize(stream_), "output copies");
+        host_filled_ = true;
     }
 }
 

@@ -101,6 +101,12 @@ public:
     bool level_counts(uint32_t level, uint32_t* out) const;
     const std::vector<std::pair<std::string, double>>& timings() const { return timings_; }
     cudaStream_t stream() const { return stream_; }
+    // Host arrays that generate() fills with octree.bin records (and LUT
+    // entries when lut != nullptr); capacity in records.  The leaf part is
+    // copied while subsampling runs.
+    void set_output_host(uint8_t* records, uint32_t* lut, uint64_t capacity);
+    bool records_filled(const void* records) const { return host_filled_ && records == host_rec_; }
+    bool lut_filled(const void* lut) const { return host_filled_ && host_lut_ && lut == host_lut_; }
     const BuildConfig& config() const { return cfg_; }
 
 private:
@@ -131,6 +137,12 @@ private:
     DevBuf g_key_, g_mask_, g_base_;   // per-block global brick tables
     DevBuf cell_keys_, spread_;         // chunking-grid boundary keys and Morton spread table
     DevBuf stage_off_, level_base_;     // staged position of each internal node's outputs; staging fill
+    uint8_t* host_rec_ = nullptr;      // caller's output arrays (set_output_host)
+    uint32_t* host_lut_ = nullptr;
+    uint64_t host_cap_ = 0;
+    bool host_filled_ = false;
+    cudaStream_t copy_stream_ = nullptr;
+    cudaEvent_t leaf_ready_ = nullptr;
     DevBuf post_ii_, node_dst_, out_total_;   // post-order of internal nodes, their output positions, P_out
     uint64_t sub_stage_cap_ = 0, sub_scratch_cap_ = 0, sub_rec_cap_ = 0;   // capacities that fit the last build
     uint32_t g_cap_ = 0, g_shift_ = 0;

@@ -25,6 +25,9 @@ struct Session {
     const uint8_t* host_cloud = nullptr;
     std::unique_ptr<oc::Builder> builder;
     std::string memory_report;
+    uint8_t* out_rec = nullptr;   // ocpi_set_output_host
+    uint32_t* out_lut = nullptr;
+    uint64_t out_cap = 0;
 
     ~Session() {
         if (!memory_report.empty() && builder) {
@@ -190,6 +193,7 @@ int ocpi_init_octree(void* session) {
         }
         s->builder.reset();
         s->builder = std::make_unique<oc::Builder>(s->cfg, s->host_cloud, s->device);
+        if (s->out_rec) s->builder->set_output_host(s->out_rec, s->out_lut, s->out_cap);
     });
 }
 
@@ -286,14 +290,26 @@ int ocpi_get_hierarchy(void* session, uint8_t* out) {
 int ocpi_get_records(void* session, uint8_t* out) {
     return execute([&] {
         if (!out) throw oc::Error("null output");
-        built(to_session(session)).copy_records(out);
+        auto& b = built(to_session(session));
+        if (!b.records_filled(out)) b.copy_records(out);   // else generate already filled it
     });
 }
 
 int ocpi_get_lut(void* session, uint32_t* out) {
     return execute([&] {
         if (!out) throw oc::Error("null output");
-        built(to_session(session)).copy_lut(out);
+        auto& b = built(to_session(session));
+        if (!b.lut_filled(out)) b.copy_lut(out);
+    });
+}
+
+int ocpi_set_output_host(void* session, uint8_t* records, uint32_t* lut, uint64_t capacity) {
+    return execute([&] {
+        auto* s = to_session(session);
+        s->out_rec = records;
+        s->out_lut = lut;
+        s->out_cap = capacity;
+        if (s->builder) s->builder->set_output_host(records, lut, capacity);
     });
 }
 

@@ -29,7 +29,7 @@ REFERENCE_SYMBOLS = [
 ADDED_SYMBOLS = [
     "ocpi_last_error", "ocpi_set_random_seed", "ocpi_set_debug_flags", "ocpi_get_stats",
     "ocpi_get_node_count", "ocpi_get_hierarchy", "ocpi_get_records", "ocpi_get_lut",
-    "ocpi_get_level_counts", "ocpi_get_timings", "ocpi_subsample_node_noalloc",
+    "ocpi_get_level_counts", "ocpi_get_timings", "ocpi_subsample_node_noalloc", "ocpi_set_output_host",
 ]
 
 HIER_DTYPE = np.dtype([("type", "u1"), ("mask", "u1"), ("points", "<u4"),
@@ -104,6 +104,7 @@ def load_library(path=LIB_PATH):
         "ocpi_get_level_counts": [vp, u32, vp],
         "ocpi_get_timings": [vp, ctypes.POINTER(ctypes.c_double), ctypes.c_int, ctypes.c_char_p, ctypes.c_int,
                              ctypes.POINTER(ctypes.c_int)],
+        "ocpi_set_output_host": [vp, vp, vp, u64],
         "ocpi_subsample_node_noalloc": [vp, u8, u32, ctypes.POINTER(d), ctypes.POINTER(d), ctypes.POINTER(d), d,
                                         u32, u64, u32, u32, u64, vp, vp, u32, vp, vp, vp, vp],
     }
@@ -211,6 +212,15 @@ class OctreeSession:
         if seed is not None:
             _check(L.ocpi_set_random_seed(h, seed), "ocpi_set_random_seed")
         _check(L.ocpi_set_debug_flags(h, debug), "ocpi_set_debug_flags")
+
+    def set_output_host(self, records, lut=None):
+        """Arrays (uint8 of 18-byte records, optional uint32 LUT) that every
+        generate fills; keep them alive (and preferably pinned)."""
+        cap = len(records) // 18
+        self._out = (records, lut)
+        _check(load_library().ocpi_set_output_host(self._h, records.ctypes.data,
+                                                   lut.ctypes.data if lut is not None else None, cap),
+               "ocpi_set_output_host")
 
     def init(self):
         _check(load_library().ocpi_init_octree(self._h), "ocpi_init_octree")

@@ -4,7 +4,7 @@ subsampling / colour-filtering mode and both record layouts."""
 import numpy as np
 import pytest
 
-from helpers import case_from_points, compare_results, make_case, run_gpu, run_oracle
+from helpers import case_from_points, compare_results, make_case, octree_api, run_gpu, run_oracle
 
 pytestmark = pytest.mark.gpu
 
@@ -163,3 +163,35 @@ def test_shuffled_point_order(cloud_type):
     case = Case(np.ascontiguousarray(recs), case.n, case.stride, case.cloud_type, case.scale, case.bb_min, case.bb_max)
     cfg = dict(chunk_grid=128, sub_grid=64, merge_threshold=3000, inter=True)
     compare_results(run_oracle(case, cfg), run_gpu(case, cfg))
+
+
+def test_output_host_arrays():
+    """Records and LUT streamed into registered host arrays during generate
+    equal the ones read back afterwards; a too-small array is an error."""
+    torch = pytest.importorskip("torch")
+    case = make_case(0, 1, 400_000, seed=41)
+    cfg = dict(chunk_grid=128, sub_grid=64, merge_threshold=3000, inter=True)
+    s = run_gpu(case, cfg)
+    n = s.stats()["points_total"]
+    cap = n + 100
+    rec = torch.empty(cap * 18, dtype=torch.uint8, pin_memory=True).numpy()
+    lut = torch.empty(cap, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
+    s.set_output_host(rec, lut)
+    for _ in range(2):
+        rec[:] = 0xAB
+        lut[:] = 0xFFFFFFFF
+        s.init()
+        s.generate()
+        # the same build read back by a fresh copy from the device
+        want_rec = s.records().view(np.uint8).reshape(-1)
+        want_lut = np.empty(n, np.uint32)
+        octree_api._check(octree_api.load_library().ocpi_get_lut(s._h, want_lut.ctypes.data), "ocpi_get_lut")
+        assert rec[: n * 18].tobytes() == want_rec.tobytes()
+        assert np.array_equal(lut[:n], want_lut)
+        assert (rec[n * 18:] == 0xAB).all()
+    small = torch.empty((case.n + 1) * 18, dtype=torch.uint8, pin_memory=True).numpy()
+    s.set_output_host(small)
+    s.init()
+    with pytest.raises(octree_api.OctreeError, match="too small"):
+        s.generate()
+    s.close()
