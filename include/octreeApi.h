@@ -117,6 +117,15 @@ OCPI_EXPORT int ocpi_get_level_counts(void* session, uint32_t level, uint32_t* o
  * values and their names (comma separated) into names (size name_bytes). */
 OCPI_EXPORT int ocpi_get_timings(void* session, double* ms, int max, char* names, int name_bytes, int* count);
 
+/* Bounding box on the device: calculateRealBB + calculateCubicBB
+ * (src/boundingbox.h:11-52, computed on the host by the reference CLI) over
+ * the cloud uploaded by ocpi_init_octree, exactly (min / max of the
+ * coordinates, NaN skipped, then the reference's cube arithmetic).  The cubic
+ * box becomes the session's bounding box, so ocpi_set_cloud_bb may be left
+ * out before ocpi_init_octree.  realBB / cubicBB (either may be NULL) receive
+ * {minX, minY, minZ, maxX, maxY, maxZ}. */
+OCPI_EXPORT int ocpi_compute_cloud_bb(void* session, double* realBB, double* cubicBB);
+
 /* Registers host arrays that every later ocpi_generate_octree fills before it
  * returns: octree.bin records (and, if lut is not NULL, the source index of
  * each record), `capacity` records each.  The leaf records are copied while

@@ -29,7 +29,7 @@ void BuildConfig::validate() const {
         throw Error("chunking grid must be a power of two in [2, 512]");
     if (sub_grid < 1 || sub_grid > 1024) throw Error("subsampling grid must be in [1, 1024]");
     if (intra && weighting) throw Error("the weighting function requires inter-cell averaging without intra-cell");
-    if (!(bb_max[0] - bb_min[0] > 0.0)) throw Error("empty bounding box");
+    if (has_bbox() && !(bb_max[0] - bb_min[0] > 0.0)) throw Error("empty bounding box");
     for (int a = 0; a < 3; ++a)
         if (!(scale[a] > 0.0)) throw Error("scale must be positive");
     if ((uint64_t)n * stride > (1ull << 40)) throw Error("cloud too large");
@@ -151,8 +151,17 @@ Builder::Builder(const BuildConfig& cfg, const uint8_t* host_cloud, int device) 
     child_first_.ensure((size_t)node_cap_ * 4);
     level_start_.ensure((depth_ + 2) * 4);
     n_nodes_.ensure(4);
+    if (cfg_.has_bbox()) build_cell_tables();
+    cloud_.ensure((size_t)cfg_.n * cfg_.stride + 64);
+    lut_.ensure((size_t)cfg_.n * 4);
+    rec_.ensure((size_t)cfg_.n * 18 + 16);   // 16 readable bytes past the last record
+    upload(host_cloud);
+}
+
+// Exact boundary keys of the chunking grid for the current bounding box, and
+// the Morton spread table.
+void Builder::build_cell_tables() {
     {
-        // exact boundary keys of the chunking grid and the Morton spread table
         const uint32_t G = cfg_.chunk_grid;
         const double t0 = (cfg_.bb_max[0] - cfg_.bb_min[0]) / G;   // kernel_helpers.cuh:14
         std::vector<uint32_t> sp(G);
@@ -171,10 +180,40 @@ Builder::Builder(const BuildConfig& cfg, const uint8_t* host_cloud, int device) 
         spread_.ensure(G * 4);
         check_cuda(cudaMemcpy(spread_.p, sp.data(), G * 4, cudaMemcpyHostToDevice), "H2D spread");
     }
-    cloud_.ensure((size_t)cfg_.n * cfg_.stride + 64);
-    lut_.ensure((size_t)cfg_.n * 4);
-    rec_.ensure((size_t)cfg_.n * 18 + 16);   // 16 readable bytes past the last record
-    upload(host_cloud);
+}
+
+// calculateRealBB + calculateCubicBB (src/boundingbox.h:11-52) over the
+// uploaded cloud; the cubic box becomes the build's bounding box.
+void Builder::compute_bbox(double real[6], double cubic[6]) {
+    bbox_keys_.ensure(6 * 8);
+    launches_ = 0;
+    launch_bbox(cloud_.as<uint8_t>(), cfg_.n, cfg_.stride, cfg_.cloud_type == 0, bbox_keys_.as<long long>(), num_sms_,
+                stream_);
+    long long k[6];
+    check_cuda(cudaMemcpyAsync(k, bbox_keys_.p, sizeof k, cudaMemcpyDeviceToHost, stream_), "D2H bbox");
+    check_cuda(cudaStreamSynchronize(stream_), "bbox");
+    for (int a = 0; a < 6; ++a) {
+        const bool lo = a < 3;
+        if (k[a] == (lo ? INT64_MAX : INT64_MIN)) {   // no finite coordinate on this axis
+            real[a] = lo ? INFINITY : -INFINITY;
+            continue;
+        }
+        real[a] = cfg_.cloud_type == 0 ? (double)host_from_key32((int32_t)k[a]) : host_from_key64((int64_t)k[a]);
+    }
+    const double dx = real[3] - real[0], dy = real[4] - real[1], dz = real[5] - real[2];
+    const double side = std::fmax(std::fmax(dx, dy), dz);
+    cubic[0] = real[0] - ((side - dx) / 2.0f);
+    cubic[1] = real[1] - ((side - dy) / 2.0f);
+    cubic[2] = real[2] - ((side - dz) / 2.0f);
+    cubic[3] = cubic[0] + side;
+    cubic[4] = cubic[1] + side;
+    cubic[5] = cubic[2] + side;
+    for (int a = 0; a < 3; ++a) {
+        cfg_.bb_min[a] = cubic[a];
+        cfg_.bb_max[a] = cubic[a + 3];
+    }
+    cfg_.validate();
+    build_cell_tables();
 }
 
 Builder::~Builder() {
@@ -246,6 +285,7 @@ void Builder::check_device_errors(const char* stage) {
 
 void Builder::generate() {
     host_filled_ = false;
+    if (!cfg_.has_bbox()) throw Error("no bounding box: call ocpi_set_cloud_bb before ocpi_init_octree or ocpi_compute_cloud_bb after it");
     if (host_rec_ && host_cap_ < cfg_.n) throw Error("output host buffer holds fewer records than the cloud");
     const double cubic = cfg_.bb_max[0] - cfg_.bb_min[0];
     CloudGrid g;

@@ -39,6 +39,12 @@ struct BuildConfig {
     uint32_t debug = 0;
 
     void validate() const;
+    // a bounding box was given (all six values zero means "not set yet")
+    bool has_bbox() const {
+        for (int a = 0; a < 3; ++a)
+            if (bb_min[a] != 0.0 || bb_max[a] != 0.0) return true;
+        return false;
+    }
 };
 
 // Grow-only device allocation.
@@ -89,6 +95,9 @@ public:
     // Uploads a new cloud of the same configuration (reuses allocations).
     void upload(const uint8_t* host_cloud);
     void generate();
+    // Real and cubic bounding boxes {minX, minY, minZ, maxX, maxY, maxZ} of
+    // the uploaded cloud; the cubic box becomes the build's bounding box.
+    void compute_bbox(double real[6], double cubic[6]);
     void export_potree(const std::string& dir) const;
     void export_json_report(const std::string& file) const;
     void export_histogram(const std::string& file, uint32_t bin_width) const;
@@ -115,6 +124,7 @@ private:
     void collect_timings();
     void check_device_errors(const char* stage);
     void build_tree_host(uint32_t n_nodes);
+    void build_cell_tables();
     void subsample();
     void compute_stats();
 
@@ -136,6 +146,7 @@ private:
     DevBuf place_src_, place_dst_, place_cnt_;
     DevBuf g_key_, g_mask_, g_base_;   // per-block global brick tables
     DevBuf cell_keys_, spread_;         // chunking-grid boundary keys and Morton spread table
+    DevBuf bbox_keys_;                  // ordered keys of the coordinate minima / maxima
     DevBuf stage_off_, level_base_;     // staged position of each internal node's outputs; staging fill
     uint8_t* host_rec_ = nullptr;      // caller's output arrays (set_output_host)
     uint32_t* host_lut_ = nullptr;

@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cstdint>
 #include <type_traits>
 
@@ -205,6 +206,60 @@ __global__ void __launch_bounds__(kCountThreads) k_count(const uint8_t* __restri
             if (m != kNoKey && ((starts >> lane) & 1u)) atomicAdd(&pyr0[m], run_end(starts) - lane);
         }
     });
+}
+
+// Coordinate minima and maxima (calculateRealBB, src/boundingbox.h:11-33) as
+// ordered keys: keys[0..2] minima, keys[3..5] maxima.  NaN coordinates are
+// skipped, as fmin / fmax skip them.  Float keys are widened to 64 bits.
+template <bool kF32>
+__global__ void __launch_bounds__(256) k_bbox(const uint8_t* __restrict__ cloud, uint64_t n, uint32_t stride,
+                                              long long* keys) {
+    long long mn[3] = {LLONG_MAX, LLONG_MAX, LLONG_MAX}, mx[3] = {LLONG_MIN, LLONG_MIN, LLONG_MIN};
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        constexpr int kWords = kF32 ? 3 : 6;
+        uint32_t w[kWords];
+        const uint8_t* rec = cloud + i * stride;
+        const uintptr_t a = reinterpret_cast<uintptr_t>(rec);
+        const uint32_t* q = reinterpret_cast<const uint32_t*>(a & ~(uintptr_t)3);
+        const uint32_t sh = (uint32_t)(a & 3) * 8;
+#pragma unroll
+        for (int j = 0; j < kWords; ++j) w[j] = __funnelshift_r(q[j], q[j + 1], sh);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            long long k;
+            bool nan;
+            if (kF32) {
+                nan = (w[c] & 0x7FFFFFFFu) > 0x7F800000u;
+                k = dev_key32(w[c]);
+            } else {
+                const uint32_t lo = w[2 * c], hi = w[2 * c + 1];
+                nan = (hi & 0x7FFFFFFFu) > 0x7FF00000u || ((hi & 0x7FFFFFFFu) == 0x7FF00000u && lo != 0);
+                k = dev_key64(lo, hi);
+            }
+            if (!nan) {
+                mn[c] = min(mn[c], k);
+                mx[c] = max(mx[c], k);
+            }
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        for (int o = 16; o > 0; o >>= 1) {
+            mn[c] = min(mn[c], (long long)__shfl_xor_sync(0xffffffffu, (unsigned long long)mn[c], o));
+            mx[c] = max(mx[c], (long long)__shfl_xor_sync(0xffffffffu, (unsigned long long)mx[c], o));
+        }
+    }
+    if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            if (mn[c] != LLONG_MAX) atomicMin(&keys[c], mn[c]);
+            if (mx[c] != LLONG_MIN) atomicMax(&keys[3 + c], mx[c]);
+        }
+    }
+}
+
+__global__ void k_bbox_init(long long* keys) {
+    if (threadIdx.x < 6) keys[threadIdx.x] = threadIdx.x < 3 ? LLONG_MAX : LLONG_MIN;
 }
 
 // Level l -> levels l+1 and l+2: one thread per level-(l+2) cell reads its 64
@@ -665,6 +720,16 @@ int launch_tag_leaves(uint32_t* pyr, const uint64_t* loff_dev, const uint32_t* l
     if (!n_leaves) return 0;
     k_tag_leaves<<<(n_leaves + 255) / 256, 256, 0, stream>>>(pyr, loff_dev, leaves, n_leaves, key, level);
     return 1;
+}
+
+int launch_bbox(const uint8_t* cloud, uint64_t n, uint32_t stride, bool float_input, long long* keys, int num_sms,
+                cudaStream_t stream) {
+    k_bbox_init<<<1, 32, 0, stream>>>(keys);
+    const uint64_t want = (n + 255) / 256;
+    const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)num_sms * 8));
+    if (float_input) k_bbox<true><<<grid, 256, 0, stream>>>(cloud, n, stride, keys);
+    else k_bbox<false><<<grid, 256, 0, stream>>>(cloud, n, stride, keys);
+    return 2;
 }
 
 int launch_push_tags(uint32_t* pyr, const uint64_t* loff_dev, uint32_t depth, uint32_t grid, uint32_t* err,

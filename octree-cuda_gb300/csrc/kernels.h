@@ -133,6 +133,12 @@ int launch_enumerate(const uint32_t* pyr, const uint64_t* level_off_dev, uint32_
 int launch_tag_leaves(uint32_t* pyr, const uint64_t* level_off_dev, const uint32_t* leaf_nodes, uint32_t n_leaves,
                        const uint32_t* key, const uint8_t* level, cudaStream_t stream);
 
+// Ordered keys of the coordinate minima (keys[0..2]) and maxima (keys[3..5])
+// of the cloud, NaN coordinates skipped (float keys widened to 64 bits);
+// LLONG_MAX / LLONG_MIN when an axis has no finite coordinate.
+int launch_bbox(const uint8_t* cloud, uint64_t n, uint32_t stride, bool float_input, long long* keys, int num_sms,
+                cudaStream_t stream);
+
 // Writes each occupied finest-level cell's leaf tag into the cell (after
 // launch_tag_leaves), so that distribution finds a point's leaf in one read.
 int launch_push_tags(uint32_t* pyr, const uint64_t* level_off_dev, uint32_t depth, uint32_t grid, uint32_t* err,

@@ -303,6 +303,21 @@ int ocpi_get_lut(void* session, uint32_t* out) {
     });
 }
 
+int ocpi_compute_cloud_bb(void* session, double* realBB, double* cubicBB) {
+    return execute([&] {
+        auto* s = to_session(session);
+        oc::check_cuda(cudaSetDevice(s->device), "cudaSetDevice");
+        double real[6], cubic[6];
+        built(s).compute_bbox(real, cubic);
+        for (int a = 0; a < 3; ++a) {
+            s->cfg.bb_min[a] = cubic[a];
+            s->cfg.bb_max[a] = cubic[a + 3];
+        }
+        if (realBB) std::memcpy(realBB, real, sizeof real);
+        if (cubicBB) std::memcpy(cubicBB, cubic, sizeof cubic);
+    });
+}
+
 int ocpi_set_output_host(void* session, uint8_t* records, uint32_t* lut, uint64_t capacity) {
     return execute([&] {
         auto* s = to_session(session);

@@ -30,6 +30,7 @@ ADDED_SYMBOLS = [
     "ocpi_last_error", "ocpi_set_random_seed", "ocpi_set_debug_flags", "ocpi_get_stats",
     "ocpi_get_node_count", "ocpi_get_hierarchy", "ocpi_get_records", "ocpi_get_lut",
     "ocpi_get_level_counts", "ocpi_get_timings", "ocpi_subsample_node_noalloc", "ocpi_set_output_host",
+    "ocpi_compute_cloud_bb",
 ]
 
 HIER_DTYPE = np.dtype([("type", "u1"), ("mask", "u1"), ("points", "<u4"),
@@ -105,6 +106,7 @@ def load_library(path=LIB_PATH):
         "ocpi_get_timings": [vp, ctypes.POINTER(ctypes.c_double), ctypes.c_int, ctypes.c_char_p, ctypes.c_int,
                              ctypes.POINTER(ctypes.c_int)],
         "ocpi_set_output_host": [vp, vp, vp, u64],
+        "ocpi_compute_cloud_bb": [vp, vp, vp],
         "ocpi_subsample_node_noalloc": [vp, u8, u32, ctypes.POINTER(d), ctypes.POINTER(d), ctypes.POINTER(d), d,
                                         u32, u64, u32, u32, u64, vp, vp, u32, vp, vp, vp, vp],
     }
@@ -189,16 +191,19 @@ class OctreeSession:
         self.close()
 
     # ---- reference call sequence
-    def set_cloud(self, cloud, *, n, stride, cloud_type, scale, bb_min, bb_max, offset=None):
+    def set_cloud(self, cloud, *, n, stride, cloud_type, scale, bb_min=None, bb_max=None, offset=None):
+        """bb_min / bb_max None: compute the box on the device after init()
+        (compute_cloud_bb)."""
         L = load_library()
         h = self._h
         _check(L.ocpi_set_cloud_type(h, cloud_type), "ocpi_set_cloud_type")
         _check(L.ocpi_set_cloud_point_amount(h, n), "ocpi_set_cloud_point_amount")
         _check(L.ocpi_set_cloud_data_stride(h, stride), "ocpi_set_cloud_data_stride")
         _check(L.ocpi_set_cloud_scale(h, *map(float, scale)), "ocpi_set_cloud_scale")
-        off = offset if offset is not None else bb_min
+        off = offset if offset is not None else (bb_min if bb_min is not None else (0.0, 0.0, 0.0))
         _check(L.ocpi_set_cloud_offset(h, *map(float, off)), "ocpi_set_cloud_offset")
-        _check(L.ocpi_set_cloud_bb(h, *map(float, bb_min), *map(float, bb_max)), "ocpi_set_cloud_bb")
+        if bb_min is not None:
+            _check(L.ocpi_set_cloud_bb(h, *map(float, bb_min), *map(float, bb_max)), "ocpi_set_cloud_bb")
         self._cloud = np.ascontiguousarray(cloud)
         _check(L.ocpi_set_point_cloud_host(h, self._cloud.ctypes.data), "ocpi_set_point_cloud_host")
 
@@ -221,6 +226,15 @@ class OctreeSession:
         _check(load_library().ocpi_set_output_host(self._h, records.ctypes.data,
                                                    lut.ctypes.data if lut is not None else None, cap),
                "ocpi_set_output_host")
+
+    def compute_cloud_bb(self):
+        """(real, cubic) bounding boxes computed on the device after init();
+        the cubic one becomes the session's bounding box."""
+        real = np.zeros(6)
+        cubic = np.zeros(6)
+        _check(load_library().ocpi_compute_cloud_bb(self._h, real.ctypes.data, cubic.ctypes.data),
+               "ocpi_compute_cloud_bb")
+        return real, cubic
 
     def init(self):
         _check(load_library().ocpi_init_octree(self._h), "ocpi_init_octree")

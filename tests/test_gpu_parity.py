@@ -195,3 +195,39 @@ def test_output_host_arrays():
     with pytest.raises(octree_api.OctreeError, match="too small"):
         s.generate()
     s.close()
+
+
+@pytest.mark.parametrize("kind,cloud_type", [(0, 0), (2, 1)])
+def test_device_bounding_box(kind, cloud_type):
+    """ocpi_compute_cloud_bb equals the CLI's host computation exactly (NaN
+    coordinates skipped), and a build on it equals the oracle's."""
+    from helpers import Case
+
+    case = make_case(kind, cloud_type, 300_000, seed=51)
+    cfg = dict(chunk_grid=128, sub_grid=64, merge_threshold=3000, inter=True)
+    ft = np.float32 if cloud_type == 0 else np.float64
+
+    def device_box(cloud):
+        s = octree_api.OctreeSession(0)
+        s.set_cloud(cloud, n=case.n, stride=case.stride, cloud_type=cloud_type, scale=case.scale)
+        s.configure(**cfg)
+        s.init()
+        real, cubic = s.compute_cloud_bb()
+        return s, cubic
+
+    # a NaN coordinate: fmin / fmax skip it
+    nan_cloud = case.cloud.copy()
+    nan_cloud[7 * case.stride: 7 * case.stride + 3 * np.dtype(ft).itemsize].view(ft)[1] = np.nan
+    s, cubic = device_box(nan_cloud)
+    want = octree_api.cubic_bbox(nan_cloud, case.n, case.stride, cloud_type)
+    assert cubic.tobytes() == np.asarray(want, np.float64).tobytes(), (cubic, want)
+    s.close()
+
+    s, cubic = device_box(case.cloud)
+    want = octree_api.cubic_bbox(case.cloud, case.n, case.stride, cloud_type)
+    assert cubic.tobytes() == np.asarray(want, np.float64).tobytes(), (cubic, want)
+    s.generate()
+    ref = run_oracle(Case(case.cloud, case.n, case.stride, cloud_type, case.scale, tuple(want[:3]), tuple(want[3:])),
+                     cfg)
+    compare_results(ref, s)
+    s.close()
