@@ -126,6 +126,21 @@ OCPI_EXPORT int ocpi_get_timings(void* session, double* ms, int max, char* names
  * {minX, minY, minZ, maxX, maxY, maxZ}. */
 OCPI_EXPORT int ocpi_compute_cloud_bb(void* session, double* realBB, double* cubicBB);
 
+/* Device memory the session holds now, in bytes (all its allocations). */
+OCPI_EXPORT int ocpi_get_device_memory(void* session, uint64_t* bytes);
+
+/* Memory estimate for a configuration, before anything is allocated (e.g. for
+ * admission): gb300Bytes is an upper bound of what a session of this library
+ * allocates (data-dependent buffers at their capacity rules, valid for every
+ * build whose output fits outputFactor * N records); referenceBytes is the
+ * reference's estimate (tools/memory_consumption.py:30-75) extended by the
+ * sparse node array, per-node counters and the weighted RGBA grid.
+ * modeFlags: OCPI_SUB_* bits (defined below).  Needs no GPU. */
+OCPI_EXPORT int ocpi_estimate_memory(uint32_t pointAmount, uint32_t dataStride, uint8_t cloudType,
+                                     uint32_t chunkingGrid, uint32_t mergingThreshold, float outputFactor,
+                                     uint32_t subsamplingGrid, uint32_t modeFlags, uint64_t* gb300Bytes,
+                                     uint64_t* referenceBytes);
+
 /* Registers host arrays that every later ocpi_generate_octree fills before it
  * returns: octree.bin records (and, if lut is not NULL, the source index of
  * each record), `capacity` records each.  The leaf records are copied while

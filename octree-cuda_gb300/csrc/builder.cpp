@@ -249,6 +249,95 @@ void Builder::collect_timings() {
     }
 }
 
+std::vector<std::pair<std::string, uint64_t>> Builder::device_allocations() const {
+    return {
+        {"cloud", cloud_.bytes},
+        {"count pyramid", pyr_.bytes},
+        {"node table", key_.bytes + count_.bytes + level_.bytes + info_.bytes + child_first_.bytes + leaves_.bytes +
+                           data_idx_.bytes + fill_.bytes + level_start_.bytes + n_nodes_.bytes + loff_.bytes +
+                           nonzero_.bytes},
+        {"octree.bin records", rec_.bytes},
+        {"LUT", lut_.bytes},
+        {"staged records", stage_rec_.bytes},
+        {"staged LUT", stage_lut_.bytes},
+        {"subsampling scratch", key_cache_.bytes + unit_cache_.bytes + acc_best_.bytes + acc_sel_.bytes +
+                                    cell_slot_.bytes + acc_intra_.bytes + acc_w_.bytes + csr_count_.bytes +
+                                    csr_start_.bytes + csr_pts_.bytes},
+        {"brick tables", g_key_.bytes + g_mask_.bytes + g_base_.bytes},
+        {"level tables", sub_nodes_.bytes + out_points_.bytes + stage_off_.bytes + post_ii_.bytes + node_dst_.bytes +
+                             place_src_.bytes + place_dst_.bytes + place_cnt_.bytes},
+        {"small", err_.bytes + work_.bytes + cell_keys_.bytes + spread_.bytes + bbox_keys_.bytes + level_base_.bytes +
+                      out_total_.bytes},
+    };
+}
+
+// Mirrors the sizing in Builder::Builder, generate() and subsample():
+// data-dependent buffers at their capacity rules (node capacity, staging and
+// final records at max(outputFactor * N, N), scratch at the staging capacity).
+uint64_t estimate_device_bytes(const BuildConfig& c, int num_sms) {
+    const uint32_t depth = ilog2(c.chunk_grid);
+    uint64_t cells = 0;
+    for (uint32_t l = 0; l <= depth; ++l) {
+        const uint64_t g = c.chunk_grid >> l;
+        cells += g * g * g;
+    }
+    uint64_t cap = 1;
+    const uint64_t per = c.n / std::max<uint32_t>(c.threshold, 1);
+    for (uint32_t l = 1; l <= depth; ++l) {
+        const uint64_t g = c.chunk_grid >> l;
+        cap += 8 * std::min<uint64_t>(g * g * g, per);
+    }
+    const uint64_t node_cap = std::min<uint64_t>(cap, cells);
+    const uint64_t out_cap = std::max<uint64_t>((uint64_t)((float)c.n * c.output_factor), c.n);
+    const bool intra = c.intra, inter = !intra && c.inter, weighted = inter && c.weighting;
+    uint64_t per_cand = 4 + 8 + 4;                      // key cache, selection key, cell list
+    if (c.random) per_cand += 4;                        // selected candidate
+    if ((intra || inter) && !weighted) per_cand += 8;   // packed colour sums
+    if (weighted) per_cand += 12 + 4 + 4 + 20;          // cell units, cell groups
+    const uint64_t bs = (c.sub_grid + 3) / 4;
+    const uint64_t bricks = std::min<uint64_t>(out_cap, bs * bs * bs);
+    uint64_t slots = 1024;
+    while (slots * 11 / 16 < bricks + 1) slots <<= 1;
+    uint64_t b = 0;
+    b += (uint64_t)c.n * c.stride + 64;                               // cloud
+    b += cells * 4;                                                    // count pyramid
+    b += node_cap * (4 + 4 + 1 + 2 + 4 + 4 + 8 + 4);                   // node table, leaf lists, fill
+    b += out_cap * (4 + 18) + 16;                                      // final LUT + records
+    b += out_cap * (4 + 18) + 64;                                      // staged LUT + records
+    b += out_cap * per_cand;                                           // subsampling scratch
+    b += (uint64_t)std::max(num_sms, 1) * slots * 16;                  // per-block brick tables
+    b += node_cap * (sizeof(SubNode) + 4 + 8 + 4 + 8 + 8 + 8 + 4);     // level tables, placement lists
+    b += 3 * (c.chunk_grid + 2) * 8 + c.chunk_grid * 4 + 64 * 256;    // keys, spread, small buffers
+    return b;
+}
+
+// tools/memory_consumption.py:30-75 (countingGrid + denseToSparseLUT +
+// tmpCounting + randomIndices + randomStates + averagingGrid + outputBuffer +
+// pointCloud + pointLut), with the configured chunking grid where the script
+// hard-codes 512, extended by the sparse node array (64 B per occupied cell,
+// bounded by the dense cell count and by N), a 4-byte counter per node and
+// the f32 RGBA grid of weighted averaging.
+uint64_t reference_estimate_bytes(const BuildConfig& c) {
+    const uint32_t depth = ilog2(c.chunk_grid);
+    uint64_t cells = 0;
+    for (uint32_t l = 0; l <= depth; ++l) {
+        const uint64_t g = c.chunk_grid >> l;
+        cells += g * g * g;
+    }
+    const double S3 = (double)c.sub_grid * c.sub_grid * c.sub_grid;
+    double b = 0;
+    b += 2.0 * cells * 4;                                   // countingGrid + denseToSparseLUT
+    b += 4;                                                 // tmpCounting
+    b += 4 * S3 + 48 * 1024;                                // randomIndices + randomStates
+    b += 8 * S3;                                            // averagingGrid
+    if (c.weighting) b += 16 * S3;                          // RGBA averaging grid
+    b += (double)c.n * 18 * c.output_factor;                // outputBuffer
+    b += (double)c.n * c.stride;                            // pointCloud
+    b += (double)c.n * c.output_factor * 4;                 // pointLut
+    b += std::min<double>((double)cells, (double)c.n) * (64 + 4);   // sparse nodes + per-node counters
+    return (uint64_t)b;
+}
+
 void Builder::set_output_host(uint8_t* records, uint32_t* lut, uint64_t capacity) {
     if (copy_stream_) check_cuda(cudaStreamSynchronize(copy_stream_), "output copies");
     host_rec_ = records;

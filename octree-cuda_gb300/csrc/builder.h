@@ -85,6 +85,12 @@ struct Stats {
     uint32_t kernel_launches = 0;   // kernels launched by the last generate
 };
 
+// Upper bound of the device memory a session allocates for a configuration
+// (the Builder's own sizing rules; data-dependent buffers at their capacity
+// rules), and the reference's estimate (tools/memory_consumption.py:30-75).
+uint64_t estimate_device_bytes(const BuildConfig& cfg, int num_sms);
+uint64_t reference_estimate_bytes(const BuildConfig& cfg);
+
 class Builder {
 public:
     Builder(const BuildConfig& cfg, const uint8_t* host_cloud, int device);
@@ -117,6 +123,8 @@ public:
     bool records_filled(const void* records) const { return host_filled_ && records == host_rec_; }
     bool lut_filled(const void* lut) const { return host_filled_ && host_lut_ && lut == host_lut_; }
     const BuildConfig& config() const { return cfg_; }
+    // Device memory held by this session: named allocations in bytes.
+    std::vector<std::pair<std::string, uint64_t>> device_allocations() const;
 
 private:
     void stage_mark(const char* name);

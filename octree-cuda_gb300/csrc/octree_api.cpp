@@ -29,12 +29,31 @@ struct Session {
     uint32_t* out_lut = nullptr;
     uint64_t out_cap = 0;
 
+    int builder_sms = 152;
+
+    // The reference's MemoryTracker writes its HTML report at process exit
+    // (memory_tracker.cuh:31-55); here each session writes its own, listing
+    // the device allocations it holds, when it is destroyed.
     ~Session() {
         if (!memory_report.empty() && builder) {
             FILE* f = std::fopen(memory_report.c_str(), "w");
             if (f) {
-                std::fprintf(f, "<html><body><pre>session device memory report\npoints %u stride %u\n</pre></body></html>\n",
-                             cfg.n, cfg.stride);
+                uint64_t total = 0;
+                std::fprintf(f, "<!DOCTYPE html>\n<html><head><title>Device memory</title></head><body>\n");
+                std::fprintf(f, "<h3>Device memory of one octree session (%u points, stride %u)</h3>\n", cfg.n,
+                             cfg.stride);
+                std::fprintf(f, "<table border=\"1\"><tr><th>allocation</th><th>bytes</th><th>MB</th></tr>\n");
+                for (const auto& a : builder->device_allocations()) {
+                    total += a.second;
+                    std::fprintf(f, "<tr><td>%s</td><td>%llu</td><td>%.3f</td></tr>\n", a.first.c_str(),
+                                 (unsigned long long)a.second, a.second / 1e6);
+                }
+                std::fprintf(f, "<tr><th>total</th><th>%llu</th><th>%.3f</th></tr>\n</table>\n",
+                             (unsigned long long)total, total / 1e6);
+                std::fprintf(f, "<p>estimate for this configuration: %llu bytes (reference formula: %llu bytes)</p>\n",
+                             (unsigned long long)oc::estimate_device_bytes(builder->config(), builder_sms),
+                             (unsigned long long)oc::reference_estimate_bytes(builder->config()));
+                std::fprintf(f, "</body></html>\n");
                 std::fclose(f);
             }
         }
@@ -193,6 +212,7 @@ int ocpi_init_octree(void* session) {
         }
         s->builder.reset();
         s->builder = std::make_unique<oc::Builder>(s->cfg, s->host_cloud, s->device);
+        cudaDeviceGetAttribute(&s->builder_sms, cudaDevAttrMultiProcessorCount, s->device);
         if (s->out_rec) s->builder->set_output_host(s->out_rec, s->out_lut, s->out_cap);
     });
 }
@@ -300,6 +320,45 @@ int ocpi_get_lut(void* session, uint32_t* out) {
         if (!out) throw oc::Error("null output");
         auto& b = built(to_session(session));
         if (!b.lut_filled(out)) b.copy_lut(out);
+    });
+}
+
+int ocpi_get_device_memory(void* session, uint64_t* bytes) {
+    return execute([&] {
+        if (!bytes) throw oc::Error("null output");
+        auto* s = to_session(session);
+        uint64_t total = 0;
+        if (s->builder)
+            for (const auto& a : s->builder->device_allocations()) total += a.second;
+        *bytes = total;
+    });
+}
+
+int ocpi_estimate_memory(uint32_t pointAmount, uint32_t dataStride, uint8_t cloudType, uint32_t chunkingGrid,
+                         uint32_t mergingThreshold, float outputFactor, uint32_t subsamplingGrid, uint32_t modeFlags,
+                         uint64_t* gb300Bytes, uint64_t* referenceBytes) {
+    return execute([&] {
+        oc::BuildConfig c;
+        c.n = pointAmount;
+        c.stride = dataStride;
+        c.cloud_type = cloudType;
+        c.chunk_grid = chunkingGrid;
+        c.threshold = mergingThreshold;
+        c.output_factor = outputFactor;
+        c.sub_grid = subsamplingGrid;
+        c.intra = (modeFlags & OCPI_SUB_INTRA) != 0;
+        c.inter = (modeFlags & OCPI_SUB_INTER) != 0;
+        c.random = (modeFlags & OCPI_SUB_RANDOM) != 0;
+        c.weighting = (modeFlags & OCPI_SUB_WEIGHTING) != 0;
+        c.validate();
+        int sms = 0, dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) {
+            cudaGetLastError();
+            sms = 152;   // GB300
+        }
+        if (gb300Bytes) *gb300Bytes = oc::estimate_device_bytes(c, sms);
+        if (referenceBytes) *referenceBytes = oc::reference_estimate_bytes(c);
     });
 }
 

@@ -30,7 +30,7 @@ ADDED_SYMBOLS = [
     "ocpi_last_error", "ocpi_set_random_seed", "ocpi_set_debug_flags", "ocpi_get_stats",
     "ocpi_get_node_count", "ocpi_get_hierarchy", "ocpi_get_records", "ocpi_get_lut",
     "ocpi_get_level_counts", "ocpi_get_timings", "ocpi_subsample_node_noalloc", "ocpi_set_output_host",
-    "ocpi_compute_cloud_bb",
+    "ocpi_compute_cloud_bb", "ocpi_get_device_memory", "ocpi_estimate_memory",
 ]
 
 HIER_DTYPE = np.dtype([("type", "u1"), ("mask", "u1"), ("points", "<u4"),
@@ -107,6 +107,9 @@ def load_library(path=LIB_PATH):
                              ctypes.POINTER(ctypes.c_int)],
         "ocpi_set_output_host": [vp, vp, vp, u64],
         "ocpi_compute_cloud_bb": [vp, vp, vp],
+        "ocpi_get_device_memory": [vp, ctypes.POINTER(u64)],
+        "ocpi_estimate_memory": [u32, u32, u8, u32, u32, ctypes.c_float, u32, u32, ctypes.POINTER(u64),
+                                 ctypes.POINTER(u64)],
         "ocpi_subsample_node_noalloc": [vp, u8, u32, ctypes.POINTER(d), ctypes.POINTER(d), ctypes.POINTER(d), d,
                                         u32, u64, u32, u32, u64, vp, vp, u32, vp, vp, vp, vp],
     }
@@ -134,6 +137,16 @@ def load_synthetic(path=SYNTH_PATH):
         S.ocsynth_cubic_bbox.restype = None
         _synth = S
     return _synth
+
+
+def estimate_memory(n, stride, cloud_type, chunk_grid=512, merge_threshold=10000, output_factor=2.2, sub_grid=128,
+                    flags=0):
+    """(upper bound of this library's device bytes, the reference's estimate)."""
+    a, b = ctypes.c_uint64(), ctypes.c_uint64()
+    _check(load_library().ocpi_estimate_memory(n, stride, cloud_type, chunk_grid, merge_threshold, output_factor,
+                                               sub_grid, flags, ctypes.byref(a), ctypes.byref(b)),
+           "ocpi_estimate_memory")
+    return a.value, b.value
 
 
 def _check(rc, what):
@@ -235,6 +248,11 @@ class OctreeSession:
         _check(load_library().ocpi_compute_cloud_bb(self._h, real.ctypes.data, cubic.ctypes.data),
                "ocpi_compute_cloud_bb")
         return real, cubic
+
+    def device_memory(self):
+        v = ctypes.c_uint64()
+        _check(load_library().ocpi_get_device_memory(self._h, ctypes.byref(v)), "ocpi_get_device_memory")
+        return v.value
 
     def init(self):
         _check(load_library().ocpi_init_octree(self._h), "ocpi_init_octree")

@@ -231,3 +231,70 @@ def test_device_bounding_box(kind, cloud_type):
                      cfg)
     compare_results(ref, s)
     s.close()
+
+
+@pytest.mark.parametrize("mode,flags", [(dict(inter=True), 2), (dict(random=True, inter=True, weighting=True), 26),
+                                        (dict(intra=True), 1)])
+def test_memory_estimate_bounds_allocations(tmp_path, mode, flags):
+    """After a build, the session's device allocations stay within
+    ocpi_estimate_memory's bound, and the memory report lists them."""
+    case = make_case(1, 0, 400_000, seed=61)
+    cfg = dict(chunk_grid=128, sub_grid=64, merge_threshold=3000, **mode)
+    s = run_gpu(case, cfg)
+    used = s.device_memory()
+    bound, ref = octree_api.estimate_memory(case.n, case.stride, case.cloud_type, 128, 3000, 2.2, 64, flags)
+    assert 0 < used <= bound, (used, bound)
+    report = tmp_path / "memory_report.html"
+    octree_api._check(octree_api.load_library().ocpi_export_memory_report(s._h, str(report).encode()), "report")
+    s.close()
+    text = report.read_text()
+    assert "count pyramid" in text and str(used) in text
+
+
+def test_potree_export_reader(tmp_path):
+    """An independent reader of the exported Potree 2.0 files: metadata,
+    hierarchy.bin entries (22 bytes, breadth-first), byte ranges that tile
+    octree.bin, and every record inside its node's cube."""
+    import json
+
+    case = make_case(0, 1, 300_000, seed=71)
+    cfg = dict(chunk_grid=128, sub_grid=64, merge_threshold=3000, inter=True)
+    s = run_gpu(case, cfg)
+    s.export_potree(str(tmp_path))
+    st = s.stats()
+    s.close()
+    meta = json.loads((tmp_path / "metadata.json").read_text())
+    hier = np.fromfile(tmp_path / "hierarchy.bin", dtype=octree_api.HIER_DTYPE)
+    recs = np.fromfile(tmp_path / "octree.bin", dtype=octree_api.RECORD_DTYPE)
+    assert octree_api.HIER_DTYPE.itemsize == 22 and octree_api.RECORD_DTYPE.itemsize == 18
+    assert meta["version"] == "2.0" and meta["points"] == st["points_total"] == len(recs)
+    assert meta["hierarchy"]["firstChunkSize"] == len(hier) * 22 == st["tree_nodes"] * 22
+    assert [a["name"] for a in meta["attributes"]] == ["position", "rgb"]
+    # node types: 0 = inner node with children, 1 = leaf
+    assert ((hier["mask"] != 0) == (hier["type"] == 0)).all() and ((hier["mask"] == 0) == (hier["type"] == 1)).all()
+    assert (hier["byte_size"] == hier["points"].astype(np.uint64) * 18).all()
+    ranges = sorted((int(o), int(o + z)) for o, z in zip(hier["byte_offset"], hier["byte_size"]) if z)
+    end = 0
+    for a, b in ranges:
+        assert a == end
+        end = b
+    assert end == len(recs) * 18
+    # breadth-first walk: node cubes relative to the bounding-box minimum
+    scale = meta["scale"][0]
+    side0 = meta["boundingBox"]["max"][0]
+    mins = np.zeros((len(hier), 3))
+    sides = np.zeros(len(hier))
+    sides[0] = side0
+    nxt = 1
+    for i in range(len(hier)):
+        for sl in range(8):
+            if int(hier["mask"][i]) & (1 << sl):
+                sides[nxt] = sides[i] / 2
+                mins[nxt] = mins[i] + sides[nxt] * np.array([(sl >> 2) & 1, (sl >> 1) & 1, sl & 1])
+                nxt += 1
+    assert nxt == len(hier)
+    xyz = np.stack([recs["x"], recs["y"], recs["z"]], axis=1).astype(np.float64) * scale
+    for i in range(len(hier)):
+        a = int(hier["byte_offset"][i]) // 18
+        p = xyz[a: a + int(hier["points"][i])]
+        assert (p >= mins[i] - 2 * scale).all() and (p <= mins[i] + sides[i] + 2 * scale).all(), i

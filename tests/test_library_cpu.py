@@ -5,6 +5,7 @@ import ctypes
 import os
 import re
 
+import numpy as np
 import pytest
 
 import octree_api
@@ -52,3 +53,25 @@ def test_noalloc_rejects_oversized_node_without_gpu():
                                        None, None, None)
     assert rc == -1
     assert b"exceed the fixed scratch limit" in L.ocpi_last_error()
+
+
+def test_memory_estimate_reference_formula():
+    """The reference estimate restates tools/memory_consumption.py:30-75 (with
+    the configured chunking grid) plus sparse nodes, counters and the RGBA
+    grid; this library's bound exceeds the data it must hold."""
+    n, stride = 119_701_547, 27
+    gb300, ref = octree_api.estimate_memory(n, stride, 1, 512, 10000, 2.2, 128, octree_api.SUB_INTER)
+    cells = sum((512 >> i) ** 3 for i in range(10))
+    s3 = 128 ** 3
+    f = float(np.float32(2.2))   # outputFactor is a float in the API
+    want = (2 * cells * 4 + 4 + 4 * s3 + 48 * 1024 + 8 * s3 + n * 18 * f + n * stride + n * f * 4
+            + min(cells, n) * 68)
+    assert abs(ref - want) <= 16, (ref, want)
+    out_cap = int(np.float32(n) * np.float32(2.2))
+    must_hold = n * stride + cells * 4 + 2 * out_cap * 22
+    assert must_hold < gb300 < 3 * must_hold
+    # more points never need less memory
+    g2, r2 = octree_api.estimate_memory(2 * n, stride, 1, 512, 10000, 2.2, 128, octree_api.SUB_INTER)
+    assert g2 > gb300 and r2 > ref
+    with pytest.raises(octree_api.OctreeError):
+        octree_api.estimate_memory(n, stride, 1, 500, 10000, 2.2, 128, 0)   # grid not a power of two
