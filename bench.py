@@ -169,7 +169,7 @@ def run_reference_arm(args):
     v = sample / t / 1e6
     line = {
         "impl": "reference", "metric": "Mpts/s octree build @120M pts", "value": round(v, 3), "unit": "Mpts/s",
-        "n_gpus": 0, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t * 1e3, 3),
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t * 1e3, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOAD, "points": N_POINTS, "sample_points": sample, **CFG},
         "cpu_baseline": {"value": round(v, 3), "unit": "Mpts/s", "cores": threads, "kind": "port",
