@@ -155,6 +155,7 @@ Builder::Builder(const BuildConfig& cfg, const uint8_t* host_cloud, int device) 
     cloud_.ensure((size_t)cfg_.n * cfg_.stride + 64);
     lut_.ensure((size_t)cfg_.n * 4);
     rec_.ensure((size_t)cfg_.n * 18 + 16);   // 16 readable bytes past the last record
+    leaf_frac_.ensure((size_t)cfg_.n * 4);
     upload(host_cloud);
 }
 
@@ -260,6 +261,7 @@ std::vector<std::pair<std::string, uint64_t>> Builder::device_allocations() cons
         {"LUT", lut_.bytes},
         {"staged records", stage_rec_.bytes},
         {"staged LUT", stage_lut_.bytes},
+        {"sub-step words", leaf_frac_.bytes + stage_frac_.bytes},
         {"subsampling scratch", key_cache_.bytes + unit_cache_.bytes + acc_best_.bytes + acc_sel_.bytes +
                                     cell_slot_.bytes + acc_intra_.bytes + acc_w_.bytes + csr_count_.bytes +
                                     csr_start_.bytes + csr_pts_.bytes},
@@ -303,7 +305,8 @@ uint64_t estimate_device_bytes(const BuildConfig& c, int num_sms) {
     b += cells * 4;                                                    // count pyramid
     b += node_cap * (4 + 4 + 1 + 2 + 4 + 4 + 8 + 4);                   // node table, leaf lists, fill
     b += out_cap * (4 + 18) + 16;                                      // final LUT + records
-    b += out_cap * (4 + 18) + 64;                                      // staged LUT + records
+    b += out_cap * (4 + 18 + 4) + 64;                                  // staged LUT + records + sub-step words
+    b += (uint64_t)c.n * 4;                                            // leaf sub-step words
     b += out_cap * per_cand;                                           // subsampling scratch
     b += (uint64_t)std::max(num_sms, 1) * slots * 16;                  // per-block brick tables
     b += node_cap * (sizeof(SubNode) + 4 + 8 + 4 + 8 + 8 + 8 + 4);     // level tables, placement lists
@@ -444,7 +447,8 @@ void Builder::generate() {
                                   err_.as<uint32_t>(), stream_);
     launches_ += launch_distribute(cloud_.as<uint8_t>(), cfg_.n, cfg_.stride, f32, g, op, pyr_.as<uint32_t>(),
                                    data_idx_.as<uint64_t>(), fill_.as<uint32_t>(), lut_.as<uint32_t>(),
-                                   rec_.as<uint8_t>(), err_.as<uint32_t>(), num_sms_, stream_);
+                                   rec_.as<uint8_t>(), leaf_frac_.as<uint32_t>(), err_.as<uint32_t>(), num_sms_,
+                                   stream_);
     stage_mark("distribute");
     check_cuda(cudaGetLastError(), "launch");
 
@@ -664,6 +668,7 @@ void Builder::subsample() {
         }
         stage_lut_.ensure(stage_cap * 4);
         stage_rec_.ensure(stage_cap * 18 + 64);
+        stage_frac_.ensure(stage_cap * 4);
         if (copy_stream_) check_cuda(cudaStreamSynchronize(copy_stream_), "output copies");
         lut_.ensure_keep(rec_cap * 4, (size_t)cfg_.n * 4, stream_);
         rec_.ensure_keep(rec_cap * 18 + 16, (size_t)cfg_.n * 18, stream_);
@@ -692,6 +697,9 @@ void Builder::subsample() {
         a.leaf_rec = rec_.as<uint8_t>();
         a.stage_lut = stage_lut_.as<uint32_t>();
         a.stage_rec = stage_rec_.as<uint8_t>();
+        a.leaf_frac = leaf_frac_.as<uint32_t>();
+        a.stage_frac = stage_frac_.as<uint32_t>();
+        a.out_frac = stage_frac_.as<uint32_t>();
         a.out_lut = stage_lut_.as<uint32_t>();
         a.out_rec = stage_rec_.as<uint8_t>();
         a.key_cache = key_cache_.as<uint32_t>();

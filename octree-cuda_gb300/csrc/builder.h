@@ -154,6 +154,7 @@ private:
     DevBuf place_src_, place_dst_, place_cnt_;
     DevBuf g_key_, g_mask_, g_base_;   // per-block global brick tables
     DevBuf cell_keys_, spread_;         // chunking-grid boundary keys and Morton spread table
+    DevBuf leaf_frac_, stage_frac_;     // sub-step words of leaf and staged records
     DevBuf bbox_keys_;                  // ordered keys of the coordinate minima / maxima
     DevBuf stage_off_, level_base_;     // staged position of each internal node's outputs; staging fill
     uint8_t* host_rec_ = nullptr;      // caller's output arrays (set_output_host)

@@ -265,8 +265,14 @@ static __device__ __noinline__ int32_t exact_out_coord(double p, double mn, doub
     return (int32_t)v;
 }
 
+// fbin receives the fractional part of (p - mn) * sf in 1/1024 steps when the
+// fast path proves it to within 2^-12 (true fraction in
+// [(fbin - 1/4) / 1024, (fbin + 5/4) / 1024]), else kNoFrac.
+constexpr uint32_t kNoFrac = 0xFFFFFFFFu;
+
 template <bool kFloatInput>
-__device__ __forceinline__ int32_t out_coord(const Coord& c, const OutAxis& o) {
+__device__ __forceinline__ int32_t out_coord_frac(const Coord& c, const OutAxis& o, uint32_t& fbin) {
+    fbin = kNoFrac;
     if (kFloatInput || c.ok) {
         // s + e1 = hi - m_hi exactly (Knuth TwoSum)
         float nm = -o.m_hi;
@@ -284,10 +290,25 @@ __device__ __forceinline__ int32_t out_coord(const Coord& c, const OutAxis& o) {
             float rem = __fsub_rn(frac, g);
             float mag = __fmaf_rn(__fadd_rn(fabsf(c.hi), fabsf(o.m_hi)), fabsf(o.sf_hi), fabsf(ph));
             float E = __fmaf_rn(mag, 2.2737367544323206e-13f, 2.384185791015625e-07f);   // 2^-42, 2^-22
-            if (rem >= E && rem <= __fsub_rn(1.0f, E)) return (int32_t)f + (int32_t)g;
+            if (rem >= E && rem <= __fsub_rn(1.0f, E)) {
+                if (E <= 2.44140625e-04f) fbin = min(__float2uint_rz(__fmul_rn(rem, 1024.0f)), 1023u);   // 2^-12
+                return (int32_t)f + (int32_t)g;
+            }
         }
     }
     return exact_out_coord(exact_value<kFloatInput>(c), o.mn, o.sf);
+}
+
+template <bool kFloatInput>
+__device__ __forceinline__ int32_t out_coord(const Coord& c, const OutAxis& o) {
+    uint32_t unused;
+    return out_coord_frac<kFloatInput>(c, o, unused);
+}
+
+// Sub-step word of an output record: bits 0-9, 10-19, 20-29 the x, y, z
+// fraction bins of out_coord_frac, bit 31 set when all three are known.
+__device__ __forceinline__ uint32_t pack_frac(uint32_t fx, uint32_t fy, uint32_t fz) {
+    return (fx == kNoFrac || fy == kNoFrac || fz == kNoFrac) ? 0u : (0x80000000u | fx | (fy << 10) | (fz << 20));
 }
 
 // ---------------------------------------------------------------------------

@@ -474,7 +474,7 @@ __global__ void __launch_bounds__(kDistThreads) k_distribute(const uint8_t* __re
                                                               const uint32_t* __restrict__ pyr0,
                                                               const uint64_t* __restrict__ data_idx, uint32_t* fill,
                                                               uint32_t* __restrict__ lut, uint8_t* __restrict__ rec,
-                                                              uint32_t* err) {
+                                                              uint32_t* __restrict__ frac, uint32_t* err) {
     extern __shared__ __align__(128) uint8_t smem[];
     const ChunkSmem L = chunk_smem(stride, g.grid, kF32, kDistTile, (kDistThreads / 32) * kStageBytes);
     load_tables<kF32>(g, smem, L);
@@ -527,10 +527,12 @@ __global__ void __launch_bounds__(kDistThreads) k_distribute(const uint8_t* __re
                             c[a] = coord_f64(__hiloint2double((int)w[2 * a + 1], (int)w[2 * a]));
                         col = w[6];
                     }
-                    const int32_t x = out_coord<kF32>(c[0], op.ax[0]);
-                    const int32_t y = out_coord<kF32>(c[1], op.ax[1]);
-                    const int32_t z = out_coord<kF32>(c[2], op.ax[2]);
+                    uint32_t fx, fy, fz;
+                    const int32_t x = out_coord_frac<kF32>(c[0], op.ax[0], fx);
+                    const int32_t y = out_coord_frac<kF32>(c[1], op.ax[1], fy);
+                    const int32_t z = out_coord_frac<kF32>(c[2], op.ax[2], fz);
                     if (x == kCoordError || y == kCoordError || z == kCoordError) set_error(err, kErrCoordRange);
+                    if (frac) frac[pos] = pack_frac(fx, fy, fz);
                     nw[0] = (uint32_t)x;
                     nw[1] = (uint32_t)y;
                     nw[2] = (uint32_t)z;
@@ -742,17 +744,18 @@ int launch_push_tags(uint32_t* pyr, const uint64_t* loff_dev, uint32_t depth, ui
 
 int launch_distribute(const uint8_t* cloud, uint64_t n, uint32_t stride, bool float_input, const CloudGrid& g,
                       const OutParams& out, const uint32_t* pyr0, const uint64_t* data_idx, uint32_t* fill,
-                      uint32_t* lut, uint8_t* rec, uint32_t* err, int num_sms, cudaStream_t stream) {
+                      uint32_t* lut, uint8_t* rec, uint32_t* frac, uint32_t* err, int num_sms,
+                      cudaStream_t stream) {
     if (n == 0) return 0;
     const size_t smem = chunk_smem(stride, g.grid, float_input, kDistTile, (kDistThreads / 32) * kStageBytes).total;
     if (float_input) {
         const int grid = chunk_grid_size(k_distribute<true>, kDistThreads, kDistTile, smem, n, num_sms);
         k_distribute<true><<<grid, kDistThreads, smem, stream>>>(cloud, n, stride, g, out, pyr0, data_idx, fill, lut,
-                                                                  rec, err);
+                                                                  rec, frac, err);
     } else {
         const int grid = chunk_grid_size(k_distribute<false>, kDistThreads, kDistTile, smem, n, num_sms);
         k_distribute<false><<<grid, kDistThreads, smem, stream>>>(cloud, n, stride, g, out, pyr0, data_idx, fill,
-                                                                   lut, rec, err);
+                                                                   lut, rec, frac, err);
     }
     return 1;
 }

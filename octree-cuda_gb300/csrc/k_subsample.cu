@@ -129,6 +129,25 @@ __device__ __forceinline__ int quant_cell(int32_t q, const QAxis& a, uint32_t G)
     return (i0 == i1 && i0 >= 0) ? i0 : -2;
 }
 
+// As quant_cell, for a candidate whose sub-step fraction bin fb (0..1023) is
+// known: the true position lies in [(fb - 1/4) / 1024, (fb + 5/4) / 1024] of
+// its quantisation step, so the interval is ~1/700 of a step wide and almost
+// never straddles a cell boundary.  The fraction terms are exact in fp32; e
+// covers the rounding of the two fused multiply-adds as in quant_cell.
+__device__ __forceinline__ int quant_cell_fine(int32_t q, uint32_t fb, const QAxis& a, uint32_t G) {
+    const int32_t dq = q - a.qn;
+    if (dq > (1 << 22) || dq < -(1 << 22)) return -2;
+    const float lo = __fmaf_rn((float)dq, a.B, a.base);
+    const float fl = __fmul_rn(__fsub_rn((float)fb, 0.25f), 9.765625e-04f);   // (fb - 1/4) / 1024
+    const float fh = __fmul_rn(__fadd_rn((float)fb, 1.25f), 9.765625e-04f);   // (fb + 5/4) / 1024
+    const float ulo = __fmaf_rn(fl, a.B, lo), uhi = __fmaf_rn(fh, a.B, lo);
+    const float e =
+        __fmul_rn(__fadd_rn(__fadd_rn(fabsf(lo), fabsf(a.base)), __fadd_rn(a.B, 4.0f)), 9.5367431640625e-07f);
+    const int i0 = idx_from_units(__fsub_rn(ulo, e), G);
+    const int i1 = idx_from_units(__fadd_rn(uhi, e), G);
+    return (i0 == i1 && i0 >= 0) ? i0 : -2;
+}
+
 // Cell-unit position used by distance weighting: the centre of the candidate's
 // quantisation step, ((q - qn) + 1/2) * B + base, in fp32.
 __device__ __forceinline__ float quant_units(int32_t q, const QAxis& a) {
@@ -366,6 +385,7 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
                 const uint32_t jbase = ns.prefix[c];
                 const uint32_t* src_lut = ((ns.kind >> c) & 1u) ? a.stage_lut : a.leaf_lut;
                 const uint16_t* src_rec = reinterpret_cast<const uint16_t*>(((ns.kind >> c) & 1u) ? a.stage_rec : a.leaf_rec);
+                const uint32_t* src_frac = ((ns.kind >> c) & 1u) ? a.stage_frac : a.leaf_frac;
                 for (uint32_t k = threadIdx.x; k < cnt; k += blockDim.x) {
                     if (*(volatile uint32_t*)&s_overflow) break;
                     const uint32_t j = jbase + k;
@@ -378,9 +398,17 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
                     const uint32_t w0 = rw[0], w1 = rw[1], w2 = rw[2], w3 = rw[3];
                     const int32_t q0 = (int32_t)__funnelshift_r(w0, w1, rs), q1 = (int32_t)__funnelshift_r(w1, w2, rs),
                                   q2 = (int32_t)__funnelshift_r(w2, w3, rs);
-                    int ix = quant_cell(q0, qa0, a.grid);
-                    int iy = quant_cell(q1, qa1, a.grid);
-                    int iz = quant_cell(q2, qa2, a.grid);
+                    const uint32_t fw = src_frac ? src_frac[start + k] : 0u;
+                    int ix, iy, iz;
+                    if (fw >> 31) {
+                        ix = quant_cell_fine(q0, fw & 1023u, qa0, a.grid);
+                        iy = quant_cell_fine(q1, (fw >> 10) & 1023u, qa1, a.grid);
+                        iz = quant_cell_fine(q2, (fw >> 20) & 1023u, qa2, a.grid);
+                    } else {
+                        ix = quant_cell(q0, qa0, a.grid);
+                        iy = quant_cell(q1, qa1, a.grid);
+                        iz = quant_cell(q2, qa2, a.grid);
+                    }
                     if ((ix | iy | iz) < 0) {
                         const uint32_t idx = src_lut[start + k];
                         Coord co[3];
@@ -603,6 +631,10 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
                     }
                 }
                 a.out_lut[oo + r] = idx;
+                if (a.out_frac) {
+                    const uint32_t* sf = ((ns.kind >> csel) & 1u) ? a.stage_frac : a.leaf_frac;
+                    a.out_frac[oo + r] = sf ? sf[spos] : 0u;
+                }
                 nw[3] = (uint32_t)cr | ((uint32_t)cg << 16);
                 nw[4] = cb;
             }

@@ -93,6 +93,11 @@ struct SubLevelArgs {
     const uint8_t* leaf_rec;    // final records (leaf part)
     const uint32_t* stage_lut;  // staging LUT of internal nodes
     const uint8_t* stage_rec;   // staging records of internal nodes
+    // sub-step words (pack_frac) beside the leaf / staged / output records;
+    // null: candidates carry none and cells are decided from q alone
+    const uint32_t* leaf_frac;
+    const uint32_t* stage_frac;
+    uint32_t* out_frac;
     uint32_t* out_lut;          // staging outputs of this level (indexed by cand_off)
     uint8_t* out_rec;
     uint32_t* out_points;       // per node: number of subsampled points
@@ -146,7 +151,8 @@ int launch_push_tags(uint32_t* pyr, const uint64_t* level_off_dev, uint32_t dept
 
 int launch_distribute(const uint8_t* cloud, uint64_t n, uint32_t stride, bool float_input, const CloudGrid& g,
                       const OutParams& out, const uint32_t* pyr0, const uint64_t* data_idx, uint32_t* fill,
-                      uint32_t* lut, uint8_t* rec, uint32_t* err, int num_sms, cudaStream_t stream);
+                      uint32_t* lut, uint8_t* rec, uint32_t* frac, uint32_t* err, int num_sms,
+                      cudaStream_t stream);
 
 // Fills the dynamic part of one level's node table before it is subsampled:
 // for children that are internal nodes (child_kind bit set, child_start = the
