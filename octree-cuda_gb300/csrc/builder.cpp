@@ -149,6 +149,10 @@ Builder::Builder(const BuildConfig& cfg, const uint8_t* host_cloud, int device) 
     level_.ensure((size_t)node_cap_);
     info_.ensure((size_t)node_cap_ * 2);
     child_first_.ensure((size_t)node_cap_ * 4);
+    data_idx_.ensure((size_t)node_cap_ * 8);
+    fill_.ensure((size_t)node_cap_ * 4);
+    check_cuda(cudaStreamCreateWithFlags(&side_stream_, cudaStreamNonBlocking), "stream");
+    check_cuda(cudaEventCreateWithFlags(&tree_ready_, cudaEventDisableTiming), "event");
     level_start_.ensure((depth_ + 2) * 4);
     n_nodes_.ensure(4);
     if (cfg_.has_bbox()) build_cell_tables();
@@ -218,6 +222,9 @@ void Builder::compute_bbox(double real[6], double cubic[6]) {
 }
 
 Builder::~Builder() {
+    if (side_stream_) cudaStreamSynchronize(side_stream_);
+    if (tree_ready_) cudaEventDestroy(tree_ready_);
+    if (side_stream_) cudaStreamDestroy(side_stream_);
     if (copy_stream_) cudaStreamSynchronize(copy_stream_);
     if (leaf_ready_) cudaEventDestroy(leaf_ready_);
     if (copy_stream_) cudaStreamDestroy(copy_stream_);
@@ -254,7 +261,7 @@ std::vector<std::pair<std::string, uint64_t>> Builder::device_allocations() cons
     return {
         {"cloud", cloud_.bytes},
         {"count pyramid", pyr_.bytes},
-        {"node table", key_.bytes + count_.bytes + level_.bytes + info_.bytes + child_first_.bytes + leaves_.bytes +
+        {"node table", key_.bytes + count_.bytes + level_.bytes + info_.bytes + child_first_.bytes +
                            data_idx_.bytes + fill_.bytes + level_start_.bytes + n_nodes_.bytes + loff_.bytes +
                            nonzero_.bytes},
         {"octree.bin records", rec_.bytes},
@@ -370,7 +377,8 @@ void Builder::check_device_errors(const char* stage) {
     if (e & kErrBelowBox) throw Error(std::string(stage) + ": a point lies below the bounding box");
     if (e & kErrCoordRange) throw Error(std::string(stage) + ": an output coordinate does not fit int32");
     if (e & kErrProbe) throw Error(std::string(stage) + ": subsampling brick table overflow");
-    if (e & kErrCapacity) throw Error(std::string(stage) + ": node capacity exceeded");
+    if (e & kErrNodeCap) throw Error(std::string(stage) + ": node capacity exceeded");
+    if (e & kErrCapacity) throw Error(std::string(stage) + ": output capacity exceeded");
     if (e & kErrTag) throw Error(std::string(stage) + ": a point found no leaf");
     if (e & kErrTimeout) throw Error(std::string(stage) + ": a bulk copy did not complete in time");
 }
@@ -410,11 +418,10 @@ void Builder::generate() {
                      node_cap_, level_start_.as<uint32_t>(), n_nodes_.as<uint32_t>(), err_.as<uint32_t>(), stream_);
     stage_mark("tree");
     check_cuda(cudaGetLastError(), "launch");
-    check_device_errors("counting");
-
-    uint32_t n_nodes = 0;
-    check_cuda(cudaMemcpy(&n_nodes, n_nodes_.p, 4, cudaMemcpyDeviceToHost), "D2H");
+    check_cuda(cudaEventRecord(tree_ready_, stream_), "event");
     if (cfg_.debug & 1) {
+        // copy of the count pyramid before the leaf tags overwrite cells
+        check_device_errors("counting");
         pyramid_copy_.assign(depth_ + 1, {});
         std::vector<uint32_t> tmp;
         for (uint32_t l = 0; l <= depth_; ++l) {
@@ -431,18 +438,12 @@ void Builder::generate() {
                         dst[x + (uint64_t)y * gl + (uint64_t)z * gl * gl] = tmp[morton3(x, y, z)];
         }
     }
-    build_tree_host(n_nodes);
 
-    // leaf tags, then distribution
-    stage_mark("host_tree");
-    std::vector<uint64_t> didx(nodes_.size(), 0);
-    for (size_t i = 0; i < nodes_.size(); ++i) didx[i] = nodes_[i].data_idx;
-    upload_vec(leaves_, leaf_ids_, stream_);
-    upload_vec(data_idx_, didx, stream_);
-    fill_.ensure(nodes_.size() * 4);
-    check_cuda(cudaMemsetAsync(fill_.p, 0, nodes_.size() * 4, stream_), "memset");
-    launches_ += launch_tag_leaves(pyr_.as<uint32_t>(), loff_.as<uint64_t>(), leaves_.as<uint32_t>(), (uint32_t)leaf_ids_.size(),
-                      key_.as<uint32_t>(), level_.as<uint8_t>(), stream_);
+    // leaf offsets and tags, then distribution: no host round trip; the host
+    // reads the node table on the side stream meanwhile
+    launches_ += launch_leaf_prep(n_nodes_.as<uint32_t>(), info_.as<uint16_t>(), count_.as<uint32_t>(),
+                                  level_.as<uint8_t>(), key_.as<uint32_t>(), pyr_.as<uint32_t>(), loff_.as<uint64_t>(),
+                                  data_idx_.as<uint64_t>(), fill_.as<uint32_t>(), cfg_.n, err_.as<uint32_t>(), stream_);
     launches_ += launch_push_tags(pyr_.as<uint32_t>(), loff_.as<uint64_t>(), depth_, cfg_.chunk_grid,
                                   err_.as<uint32_t>(), stream_);
     launches_ += launch_distribute(cloud_.as<uint8_t>(), cfg_.n, cfg_.stride, f32, g, op, pyr_.as<uint32_t>(),
@@ -451,6 +452,7 @@ void Builder::generate() {
                                    stream_);
     stage_mark("distribute");
     check_cuda(cudaGetLastError(), "launch");
+    build_tree_host();
 
     subsample();   // also places the internal nodes' records (stage marks "sub_l*", "place")
     check_cuda(cudaGetLastError(), "launch");
@@ -459,15 +461,28 @@ void Builder::generate() {
     compute_stats();
 }
 
-void Builder::build_tree_host(uint32_t n) {
+// Host copy of the node table (NodeHost), read on the side stream once tree
+// enumeration is done, while distribution runs on the build stream.
+void Builder::build_tree_host() {
+    check_cuda(cudaStreamWaitEvent(side_stream_, tree_ready_, 0), "wait");
+    uint32_t n = 0, e = 0;
+    check_cuda(cudaMemcpyAsync(&n, n_nodes_.p, 4, cudaMemcpyDeviceToHost, side_stream_), "D2H");
+    check_cuda(cudaMemcpyAsync(&e, err_.p, 4, cudaMemcpyDeviceToHost, side_stream_), "D2H");
+    check_cuda(cudaStreamSynchronize(side_stream_), "tree");
+    if (e & kErrNodeCap) {
+        check_cuda(cudaStreamSynchronize(stream_), "tree");
+        throw Error("counting: node capacity exceeded");
+    }
+    if (n > node_cap_) throw Error("counting: node count out of range");
     std::vector<uint32_t> key(n), count(n), child_first(n);
     std::vector<uint8_t> level(n);
     std::vector<uint16_t> info(n);
-    check_cuda(cudaMemcpy(key.data(), key_.p, n * 4, cudaMemcpyDeviceToHost), "D2H");
-    check_cuda(cudaMemcpy(count.data(), count_.p, n * 4, cudaMemcpyDeviceToHost), "D2H");
-    check_cuda(cudaMemcpy(child_first.data(), child_first_.p, n * 4, cudaMemcpyDeviceToHost), "D2H");
-    check_cuda(cudaMemcpy(level.data(), level_.p, n, cudaMemcpyDeviceToHost), "D2H");
-    check_cuda(cudaMemcpy(info.data(), info_.p, n * 2, cudaMemcpyDeviceToHost), "D2H");
+    check_cuda(cudaMemcpyAsync(key.data(), key_.p, n * 4, cudaMemcpyDeviceToHost, side_stream_), "D2H");
+    check_cuda(cudaMemcpyAsync(count.data(), count_.p, n * 4, cudaMemcpyDeviceToHost, side_stream_), "D2H");
+    check_cuda(cudaMemcpyAsync(child_first.data(), child_first_.p, n * 4, cudaMemcpyDeviceToHost, side_stream_), "D2H");
+    check_cuda(cudaMemcpyAsync(level.data(), level_.p, n, cudaMemcpyDeviceToHost, side_stream_), "D2H");
+    check_cuda(cudaMemcpyAsync(info.data(), info_.p, n * 2, cudaMemcpyDeviceToHost, side_stream_), "D2H");
+    check_cuda(cudaStreamSynchronize(side_stream_), "tree");
     nodes_.assign(n, NodeHost{});
     leaf_ids_.clear();
     internal_by_level_.assign(depth_ + 1, {});

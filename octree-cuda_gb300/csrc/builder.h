@@ -131,7 +131,7 @@ private:
     void stage_begin();
     void collect_timings();
     void check_device_errors(const char* stage);
-    void build_tree_host(uint32_t n_nodes);
+    void build_tree_host();
     void build_cell_tables();
     void subsample();
     void compute_stats();
@@ -146,7 +146,7 @@ private:
 
     DevBuf cloud_, pyr_, loff_, err_, nonzero_;
     DevBuf key_, count_, level_, info_, child_first_, level_start_, n_nodes_;
-    DevBuf leaves_, data_idx_, fill_;
+    DevBuf data_idx_, fill_;
     DevBuf lut_, rec_;                  // final outputs (N + P_out records)
     DevBuf stage_lut_, stage_rec_;      // staged internal outputs
     DevBuf sub_nodes_, out_points_, work_;
@@ -162,6 +162,8 @@ private:
     uint64_t host_cap_ = 0;
     bool host_filled_ = false;
     cudaStream_t copy_stream_ = nullptr;
+    cudaStream_t side_stream_ = nullptr;   // reads the node table while distribution runs
+    cudaEvent_t tree_ready_ = nullptr;
     cudaEvent_t leaf_ready_ = nullptr;
     DevBuf post_ii_, node_dst_, out_total_;   // post-order of internal nodes, their output positions, P_out
     uint64_t sub_stage_cap_ = 0, sub_scratch_cap_ = 0, sub_rec_cap_ = 0;   // capacities that fit the last build

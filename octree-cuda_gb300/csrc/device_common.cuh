@@ -125,6 +125,7 @@ enum : uint32_t {
     kErrCapacity = 1u << 3,      // a scratch buffer was too small
     kErrTag = 1u << 4,           // a point found no leaf
     kErrTimeout = 1u << 5,       // a bounded wait on a bulk copy gave up
+    kErrNodeCap = 1u << 6,       // the tree has more nodes than the node table holds
 };
 
 // ---------------------------------------------------------------------------

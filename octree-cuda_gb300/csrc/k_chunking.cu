@@ -402,7 +402,7 @@ __global__ void __launch_bounds__(1024) k_enumerate(const uint32_t* __restrict__
             __syncthreads();
             if (threadIdx.x == 0) {
                 s_next = next + total;
-                if (s_next > cap) set_error(err, kErrCapacity);
+                if (s_next > cap) set_error(err, kErrNodeCap);
             }
             __syncthreads();
             if (s_next > cap) return;
@@ -422,12 +422,34 @@ __global__ void __launch_bounds__(1024) k_enumerate(const uint32_t* __restrict__
     }
 }
 
-__global__ void k_tag_leaves(uint32_t* pyr, const uint64_t* __restrict__ loff, const uint32_t* __restrict__ leaves,
-                             uint32_t n_leaves, const uint32_t* __restrict__ key, const uint8_t* __restrict__ level) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n_leaves) return;
-    uint32_t node = leaves[i];
-    pyr[loff[level[node]] + key[node]] = kLeafTag | node;
+// Leaf data offsets and leaf tags from the node table, without the host: one
+// block scans the nodes in BFS order.  Leaf i gets data_idx = the points of
+// the leaves before it (hierarchy BFS order), its pyramid cell the tag
+// kLeafTag | i, and its fill counter 0.  Skipped when the node table
+// overflowed; flags kErrTag when the leaves do not hold all n_points.
+__global__ void __launch_bounds__(1024) k_leaf_prep(const uint32_t* __restrict__ n_nodes_p,
+                                                    const uint16_t* __restrict__ info, const uint32_t* __restrict__ count,
+                                                    const uint8_t* __restrict__ level, const uint32_t* __restrict__ key,
+                                                    uint32_t* pyr, const uint64_t* __restrict__ loff, uint64_t* data_idx,
+                                                    uint32_t* fill, uint64_t n_points, uint32_t* err) {
+    __shared__ uint64_t warp_sums[32];
+    if (*err & kErrNodeCap) return;
+    const uint32_t n = *n_nodes_p;
+    uint64_t running = 0;
+    for (uint32_t k0 = 0; k0 < n; k0 += blockDim.x) {
+        const uint32_t i = k0 + threadIdx.x;
+        const bool leaf = i < n && !(info[i] & 1);
+        const uint64_t c = leaf ? count[i] : 0;
+        uint64_t tot;
+        const uint64_t pre = block_exclusive_scan64(c, warp_sums, tot);
+        if (i < n) {
+            fill[i] = 0;
+            data_idx[i] = leaf ? running + pre : 0;
+            if (leaf) pyr[loff[level[i]] + key[i]] = kLeafTag | i;
+        }
+        running += tot;
+    }
+    if (threadIdx.x == 0 && running != n_points) set_error(err, kErrTag);
 }
 
 // Writes the leaf tag of every occupied finest cell into the cell: one
@@ -513,7 +535,7 @@ __global__ void __launch_bounds__(kDistThreads) k_distribute(const uint8_t* __re
             if (node != kNoKey) {
                 const uint64_t pos = first + (lane - leader);
                 if (pos >= n) {   // only reachable with corrupted input tags
-                    set_error(err, kErrCapacity);
+                    set_error(err, kErrTag);
                 } else {
                     ok = true;
                     lut[pos] = (uint32_t)(p0 + k);
@@ -717,13 +739,6 @@ int launch_enumerate(const uint32_t* pyr, const uint64_t* loff_dev, uint32_t dep
     return 1;
 }
 
-int launch_tag_leaves(uint32_t* pyr, const uint64_t* loff_dev, const uint32_t* leaves, uint32_t n_leaves,
-                       const uint32_t* key, const uint8_t* level, cudaStream_t stream) {
-    if (!n_leaves) return 0;
-    k_tag_leaves<<<(n_leaves + 255) / 256, 256, 0, stream>>>(pyr, loff_dev, leaves, n_leaves, key, level);
-    return 1;
-}
-
 int launch_bbox(const uint8_t* cloud, uint64_t n, uint32_t stride, bool float_input, long long* keys, int num_sms,
                 cudaStream_t stream) {
     k_bbox_init<<<1, 32, 0, stream>>>(keys);
@@ -732,6 +747,13 @@ int launch_bbox(const uint8_t* cloud, uint64_t n, uint32_t stride, bool float_in
     if (float_input) k_bbox<true><<<grid, 256, 0, stream>>>(cloud, n, stride, keys);
     else k_bbox<false><<<grid, 256, 0, stream>>>(cloud, n, stride, keys);
     return 2;
+}
+
+int launch_leaf_prep(const uint32_t* n_nodes, const uint16_t* info, const uint32_t* count, const uint8_t* level,
+                     const uint32_t* key, uint32_t* pyr, const uint64_t* loff_dev, uint64_t* data_idx, uint32_t* fill,
+                     uint64_t n_points, uint32_t* err, cudaStream_t stream) {
+    k_leaf_prep<<<1, 1024, 0, stream>>>(n_nodes, info, count, level, key, pyr, loff_dev, data_idx, fill, n_points, err);
+    return 1;
 }
 
 int launch_push_tags(uint32_t* pyr, const uint64_t* loff_dev, uint32_t depth, uint32_t grid, uint32_t* err,

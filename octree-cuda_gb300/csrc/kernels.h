@@ -135,17 +135,20 @@ int launch_enumerate(const uint32_t* pyr, const uint64_t* level_off_dev, uint32_
                       uint32_t* key, uint32_t* count, uint8_t* level, uint16_t* info, uint32_t* child_first,
                       uint32_t cap, uint32_t* level_start, uint32_t* n_nodes, uint32_t* err, cudaStream_t stream);
 
-int launch_tag_leaves(uint32_t* pyr, const uint64_t* level_off_dev, const uint32_t* leaf_nodes, uint32_t n_leaves,
-                       const uint32_t* key, const uint8_t* level, cudaStream_t stream);
-
 // Ordered keys of the coordinate minima (keys[0..2]) and maxima (keys[3..5])
 // of the cloud, NaN coordinates skipped (float keys widened to 64 bits);
 // LLONG_MAX / LLONG_MIN when an axis has no finite coordinate.
 int launch_bbox(const uint8_t* cloud, uint64_t n, uint32_t stride, bool float_input, long long* keys, int num_sms,
                 cudaStream_t stream);
 
+// Leaf data offsets (BFS order), leaf tags in the pyramid and cleared fill
+// counters, computed on the device from the enumerated node table.
+int launch_leaf_prep(const uint32_t* n_nodes, const uint16_t* info, const uint32_t* count, const uint8_t* level,
+                     const uint32_t* key, uint32_t* pyr, const uint64_t* loff_dev, uint64_t* data_idx, uint32_t* fill,
+                     uint64_t n_points, uint32_t* err, cudaStream_t stream);
+
 // Writes each occupied finest-level cell's leaf tag into the cell (after
-// launch_tag_leaves), so that distribution finds a point's leaf in one read.
+// launch_leaf_prep), so that distribution finds a point's leaf in one read.
 int launch_push_tags(uint32_t* pyr, const uint64_t* level_off_dev, uint32_t depth, uint32_t grid, uint32_t* err,
                      cudaStream_t stream);
 
