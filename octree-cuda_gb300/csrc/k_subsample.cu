@@ -21,6 +21,7 @@
 //           coordinates of the chosen point, staged record.
 //
 // All neighbour lookups of the 3x3x3 filters go through the shared brick map.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -309,30 +310,55 @@ struct WeightedSum {
     }
 };
 
-// kColor: 0 raw colour, 1 intra-cell, 2 inter-cell, 3 distance-weighted inter-cell
-template <bool kF32, int kColor, bool kRandom>
+// kColor: 0 raw colour, 1 intra-cell, 2 inter-cell, 3 distance-weighted inter-cell.
+// kCluster: a thread-block cluster shares each node (levels with fewer nodes
+// than SMs).  The brick map, its counters and the node's cell count live in
+// the shared memory of cluster rank 0 and the other blocks reach them through
+// distributed shared memory; candidates and cells are split over all blocks
+// of the cluster, and cluster barriers separate the phases.
+template <bool kF32, int kColor, bool kRandom, bool kCluster>
 __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
+    static_assert(!(kCluster && kColor == 3), "weighted averaging runs one block per node");
+    namespace cg = cooperative_groups;
     extern __shared__ uint64_t dyn[];
     __shared__ NodeShared ns;
     __shared__ uint32_t warp_sums[32];
     __shared__ uint32_t s_bricks, s_overflow;
+    const uint32_t csize = kCluster ? cg::this_cluster().num_blocks() : 1u;
+    const uint32_t crank = kCluster ? cg::this_cluster().block_rank() : 0u;
+    const uint32_t tid0 = crank * blockDim.x + threadIdx.x;   // this thread's index within the node's workers
+    const uint32_t tstride = csize * blockDim.x;
+    auto sync_all = [&]() {
+        if constexpr (kCluster) cg::this_cluster().sync();
+        else __syncthreads();
+    };
+    // rank 0's copies (this block's own when not clustered)
+    auto owner = [&](auto* p) {
+        if constexpr (kCluster) return cg::this_cluster().map_shared_rank(p, 0);
+        else return p;
+    };
+    NodeShared* ns0 = owner(&ns);
+    uint32_t* p_bricks = owner(&s_bricks);
+    uint32_t* p_overflow = owner(&s_overflow);
+    uint64_t* dyn0 = owner(dyn);
     BrickMap sm_map;
     // per-warp staging area of the emitted records, after the brick table
     uint8_t* stage = reinterpret_cast<uint8_t*>(dyn + 2 * kBrickSlots) + (threadIdx.x >> 5) * kStageBytes;
-    sm_map.mask = dyn;
-    sm_map.key = reinterpret_cast<uint32_t*>(dyn + kBrickSlots);
+    sm_map.mask = dyn0;
+    sm_map.key = reinterpret_cast<uint32_t*>(dyn0 + kBrickSlots);
     sm_map.base = sm_map.key + kBrickSlots;
     sm_map.cap = kBrickSlots;
     sm_map.shift = kBrickShift;
     sm_map.grid = a.grid;
     sm_map.bs = (a.grid + 3) >> 2;
-    // per-block brick table in global memory for nodes that outgrow shared memory
+    // per-block (per-cluster) brick table in global memory for nodes that outgrow shared memory
+    const uint64_t owner_block = blockIdx.x / csize;
     BrickMap gl_map = sm_map;
     gl_map.cap = a.global_cap;
     gl_map.shift = a.global_shift;
-    gl_map.mask = a.global_mask + (uint64_t)blockIdx.x * a.global_cap;
-    gl_map.key = a.global_key + (uint64_t)blockIdx.x * a.global_cap;
-    gl_map.base = a.global_base + (uint64_t)blockIdx.x * a.global_cap;
+    gl_map.mask = a.global_mask + owner_block * a.global_cap;
+    gl_map.key = a.global_key + owner_block * a.global_cap;
+    gl_map.base = a.global_base + owner_block * a.global_cap;
 
     constexpr bool intra = kColor == 1;
     constexpr bool inter = kColor >= 2;
@@ -341,10 +367,13 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
     constexpr bool averaged = intra || inter;
 
     for (;;) {
-        if (threadIdx.x == 0) ns.node = atomicAdd(a.work_counter, 1u);
-        __syncthreads();
-        const uint32_t ni = ns.node;
-        if (ni >= a.n_nodes) break;
+        if (crank == 0 && threadIdx.x == 0) ns.node = atomicAdd(a.work_counter, 1u);
+        sync_all();
+        const uint32_t ni = ns0->node;
+        if (ni >= a.n_nodes) {
+            sync_all();   // rank 0's shared memory stays valid until every block has read it
+            break;
+        }
         const SubNode& nd = a.nodes[ni];
         if (threadIdx.x == 0) {
             ns.nchild = nd.nchild;
@@ -369,15 +398,15 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
         // ---- pass A: cells and occupancy.  A node whose bricks exceed 70% of
         // the shared table is redone with the block's global-memory table.
         for (int attempt = 0; attempt < 2; ++attempt) {
-            for (uint32_t i = threadIdx.x; i < bm.cap; i += blockDim.x) {
+            for (uint32_t i = tid0; i < bm.cap; i += tstride) {
                 bm.key[i] = 0;
                 bm.mask[i] = 0;
             }
-            if (threadIdx.x == 0) {
+            if (crank == 0 && threadIdx.x == 0) {
                 s_bricks = 0;
                 s_overflow = 0;
             }
-            __syncthreads();
+            sync_all();
             const uint32_t limit = bm.cap - (bm.cap >> 2) - (bm.cap >> 4);
             for (uint32_t c = 0; c < ns.nchild; ++c) {
                 const uint32_t cnt = ns.count[c];
@@ -386,8 +415,8 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
                 const uint32_t* src_lut = ((ns.kind >> c) & 1u) ? a.stage_lut : a.leaf_lut;
                 const uint16_t* src_rec = reinterpret_cast<const uint16_t*>(((ns.kind >> c) & 1u) ? a.stage_rec : a.leaf_rec);
                 const uint32_t* src_frac = ((ns.kind >> c) & 1u) ? a.stage_frac : a.leaf_frac;
-                for (uint32_t k = threadIdx.x; k < cnt; k += blockDim.x) {
-                    if (*(volatile uint32_t*)&s_overflow) break;
+                for (uint32_t k = tid0; k < cnt; k += tstride) {
+                    if (*(volatile uint32_t*)p_overflow) break;
                     const uint32_t j = jbase + k;
                     // cell from the record's quantised coordinates; the cloud point
                     // is read only when a quantisation step straddles a boundary
@@ -429,9 +458,9 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
                     uint32_t bit = (ix & 3) | ((iy & 3) << 2) | ((iz & 3) << 4);
                     bool fresh;
                     uint32_t slot = brick_insert(bm, b + 1, fresh);
-                    if (fresh && atomicAdd(&s_bricks, 1u) + 1 >= limit) s_overflow = 1;
+                    if (fresh && atomicAdd(p_bricks, 1u) + 1 >= limit) *(volatile uint32_t*)p_overflow = 1;
                     if (slot >= bm.cap) {
-                        s_overflow = 1;
+                        *(volatile uint32_t*)p_overflow = 1;
                         break;
                     }
                     // 32-bit atomic on the half of the mask that holds the bit
@@ -444,24 +473,24 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
                     }
                 }
             }
-            __syncthreads();
-            if (!s_overflow) break;
+            sync_all();
+            if (!*(volatile uint32_t*)p_overflow) break;
             if (attempt == 1 || bm.key == gl_map.key) {
-                if (threadIdx.x == 0) atomicOr(a.err, kErrProbe);
+                if (crank == 0 && threadIdx.x == 0) atomicOr(a.err, kErrProbe);
                 break;
             }
             bm = gl_map;
-            __syncthreads();
+            sync_all();
         }
-        const bool failed = s_overflow != 0;
-        __syncthreads();
+        const bool failed = *(volatile uint32_t*)p_overflow != 0;
+        sync_all();
         if (failed) {
-            if (threadIdx.x == 0) a.out_points[ni] = 0;
+            if (crank == 0 && threadIdx.x == 0) a.out_points[ni] = 0;
             continue;
         }
 
-        // ---- ranks of occupied cells (each thread scans a run of slots)
-        {
+        // ---- ranks of occupied cells (each thread of rank 0 scans a run of slots)
+        if (crank == 0) {
             const uint32_t per = (bm.cap + blockDim.x - 1) / blockDim.x;
             const uint32_t first = threadIdx.x * per;
             const uint32_t last = min(first + per, bm.cap);
@@ -475,9 +504,9 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
             }
             if (threadIdx.x == 0) ns.cells = total;
         }
-        __syncthreads();
+        sync_all();
         // rank -> (brick slot, bit), for the per-cell emit
-        for (uint32_t k = threadIdx.x; k < bm.cap; k += blockDim.x) {
+        for (uint32_t k = tid0; k < bm.cap; k += tstride) {
             uint64_t m = bm.mask[k];
             uint32_t r = bm.base[k];
             while (m) {
@@ -486,13 +515,13 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
                 a.cell_slot[off + r++] = (k << 6) | bit;
             }
         }
-        const uint32_t cells = ns.cells;
-        for (uint32_t r = threadIdx.x; r < cells; r += blockDim.x) {
+        const uint32_t cells = ns0->cells;
+        for (uint32_t r = tid0; r < cells; r += tstride) {
             a.acc_best[off + r] = ~0ull;
             if (averaged && !weighted) a.acc_intra[off + r] = 0;
             if (weighted) a.csr_count[off + r] = 0;
         }
-        __syncthreads();
+        sync_all();
 
         // ---- pass B: selection and colour sums
         for (uint32_t c = 0; c < ns.nchild; ++c) {
@@ -502,7 +531,7 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
             const bool staged = (ns.kind >> c) & 1u;
             const uint32_t* src_lut = staged ? a.stage_lut : a.leaf_lut;
             const uint8_t* src_rec = staged ? a.stage_rec : a.leaf_rec;
-            for (uint32_t k = threadIdx.x; k < cnt; k += blockDim.x) {
+            for (uint32_t k = tid0; k < cnt; k += tstride) {
                 const uint32_t kc = a.key_cache[off + jbase + k];
                 const uint32_t slot = kc >> 6, bit = kc & 63;
                 const uint32_t rank = bm.base[slot] + (uint32_t)__popcll(bm.mask[slot] & ((1ull << bit) - 1ull));
@@ -527,7 +556,7 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
                 if (weighted) atomicAdd(&a.csr_count[off + rank], 1u);
             }
         }
-        __syncthreads();
+        sync_all();
 
         // ---- explicit random: the candidate holding each cell's winning key
         if constexpr (random) {
@@ -536,7 +565,7 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
                 const uint64_t start = ns.start[c];
                 const uint32_t jbase = ns.prefix[c];
                 const uint32_t* src_lut = ((ns.kind >> c) & 1u) ? a.stage_lut : a.leaf_lut;
-                for (uint32_t k = threadIdx.x; k < cnt; k += blockDim.x) {
+                for (uint32_t k = tid0; k < cnt; k += tstride) {
                     uint32_t kc = a.key_cache[off + jbase + k];
                     uint32_t slot = kc >> 6, bit = kc & 63;
                     uint32_t rank = bm.base[slot] + (uint32_t)__popcll(bm.mask[slot] & ((1ull << bit) - 1ull));
@@ -544,7 +573,7 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
                     if ((uint32_t)a.acc_best[off + rank] == idx) a.acc_sel[off + rank] = jbase + k;
                 }
             }
-            __syncthreads();
+            sync_all();
         }
 
         // ---- weighted: group candidates by cell (CSR)
@@ -587,7 +616,7 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
 
         // ---- emit one record per occupied cell (thread per cell, rank order;
         // each warp writes 32 consecutive records with coalesced stores)
-        for (uint32_t r0 = threadIdx.x & ~31u; r0 < cells; r0 += blockDim.x) {
+        for (uint32_t r0 = tid0 & ~31u; r0 < cells; r0 += tstride) {
             const uint32_t r = r0 + (threadIdx.x & 31);
             uint32_t nw[5] = {0, 0, 0, 0, 0};
             if (r < cells) {
@@ -640,8 +669,8 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
             }
             store_run(a.out_rec + (oo + r0) * 18, 0, min(32u, cells - r0), nw, stage);
         }
-        if (threadIdx.x == 0) a.out_points[ni] = cells;
-        __syncthreads();
+        if (crank == 0 && threadIdx.x == 0) a.out_points[ni] = cells;
+        sync_all();
     }
 }
 
@@ -709,28 +738,64 @@ size_t subsample_smem_bytes() {
 
 namespace {
 
+// Blocks per node for a level of n_nodes nodes: one while the level fills
+// half the SMs, else a power-of-two cluster of up to 8 blocks.
+uint32_t cluster_size(uint32_t n_nodes, int num_sms) {
+    if (2 * n_nodes >= (uint32_t)num_sms) return 1;
+    uint32_t c = 1;
+    while (c < 8 && 2 * c * n_nodes <= (uint32_t)num_sms) c <<= 1;
+    return c;
+}
+
 template <bool kF32, int kColor, bool kRandom>
-void launch_one(const SubLevelArgs& a, int grid, size_t smem, cudaStream_t stream) {
-    cudaFuncSetAttribute(k_subsample<kF32, kColor, kRandom>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_subsample<kF32, kColor, kRandom><<<grid, kSubThreads, smem, stream>>>(a);
+void launch_one(const SubLevelArgs& a, int num_sms, size_t smem, cudaStream_t stream) {
+    constexpr bool kCanCluster = kColor != 3;
+    const uint32_t cs = kCanCluster ? cluster_size(a.n_nodes, num_sms) : 1u;
+    if (cs > 1) {
+        auto kern = k_subsample<kF32, kColor, kRandom, kCanCluster>;
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = cs;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.blockDim = dim3(kSubThreads);
+        cfg.dynamicSmemBytes = smem;
+        cfg.stream = stream;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        cfg.gridDim = dim3(cs);
+        int max_clusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&max_clusters, kern, &cfg) == cudaSuccess && max_clusters > 0) {
+            const uint32_t clusters = std::min<uint32_t>(a.n_nodes, (uint32_t)max_clusters);
+            cfg.gridDim = dim3(clusters * cs);
+            if (cudaLaunchKernelEx(&cfg, kern, a) == cudaSuccess) return;
+        }
+        cudaGetLastError();   // no cluster of this size fits: one block per node
+    }
+    auto kern = k_subsample<kF32, kColor, kRandom, false>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const int grid = (int)std::min<uint32_t>(a.n_nodes, (uint32_t)num_sms);
+    kern<<<grid, kSubThreads, smem, stream>>>(a);
 }
 
 template <bool kF32>
-void launch_mode(const SubLevelArgs& a, int grid, size_t smem, cudaStream_t stream) {
+void launch_mode(const SubLevelArgs& a, int num_sms, size_t smem, cudaStream_t stream) {
     const bool intra = (a.mode & kModeIntra) != 0;
     const bool inter = !intra && (a.mode & kModeInter) != 0;
     const bool weighted = inter && (a.mode & kModeWeight) != 0;
     const int color = intra ? 1 : (weighted ? 3 : (inter ? 2 : 0));
     const bool random = (a.mode & kModeRandom) != 0;
     switch (color * 2 + (random ? 1 : 0)) {
-    case 0: launch_one<kF32, 0, false>(a, grid, smem, stream); break;
-    case 1: launch_one<kF32, 0, true>(a, grid, smem, stream); break;
-    case 2: launch_one<kF32, 1, false>(a, grid, smem, stream); break;
-    case 3: launch_one<kF32, 1, true>(a, grid, smem, stream); break;
-    case 4: launch_one<kF32, 2, false>(a, grid, smem, stream); break;
-    case 5: launch_one<kF32, 2, true>(a, grid, smem, stream); break;
-    case 6: launch_one<kF32, 3, false>(a, grid, smem, stream); break;
-    default: launch_one<kF32, 3, true>(a, grid, smem, stream); break;
+    case 0: launch_one<kF32, 0, false>(a, num_sms, smem, stream); break;
+    case 1: launch_one<kF32, 0, true>(a, num_sms, smem, stream); break;
+    case 2: launch_one<kF32, 1, false>(a, num_sms, smem, stream); break;
+    case 3: launch_one<kF32, 1, true>(a, num_sms, smem, stream); break;
+    case 4: launch_one<kF32, 2, false>(a, num_sms, smem, stream); break;
+    case 5: launch_one<kF32, 2, true>(a, num_sms, smem, stream); break;
+    case 6: launch_one<kF32, 3, false>(a, num_sms, smem, stream); break;
+    default: launch_one<kF32, 3, true>(a, num_sms, smem, stream); break;
     }
 }
 
@@ -739,9 +804,8 @@ void launch_mode(const SubLevelArgs& a, int grid, size_t smem, cudaStream_t stre
 int launch_subsample_level(const SubLevelArgs& a, int num_sms, cudaStream_t stream) {
     if (!a.n_nodes) return 0;
     size_t smem = subsample_smem_bytes();
-    int grid = (int)std::min<uint32_t>(a.n_nodes, (uint32_t)num_sms);
-    if (a.float_input) launch_mode<true>(a, grid, smem, stream);
-    else launch_mode<false>(a, grid, smem, stream);
+    if (a.float_input) launch_mode<true>(a, num_sms, smem, stream);
+    else launch_mode<false>(a, num_sms, smem, stream);
     return 1;
 }
 
