@@ -152,6 +152,63 @@ OCPI_EXPORT int ocpi_estimate_memory(uint32_t pointAmount, uint32_t dataStride, 
  * reference can hold).  records = NULL unregisters. */
 OCPI_EXPORT int ocpi_set_output_host(void* session, uint8_t* records, uint32_t* lut, uint64_t capacity);
 
+/* ---- batched and served forms (no counterpart in the reference) ---------
+ *
+ * An executor runs independent builds at once on one GPU: `lanes` worker
+ * threads, each with its own builder, streams and grow-only buffers (a lane
+ * reuses its buffers from job to job, so a warm executor allocates nothing).
+ * Admission: a job's device memory is bounded as by ocpi_estimate_memory; a
+ * lane reserves the largest bound it has run, and a job starts only while the
+ * lanes' reservations fit memoryBudget (oldest fitting job first; an idle
+ * lane gives its memory back when a waiting job needs it).  A job whose bound
+ * alone exceeds the budget is refused at submission.  Each result equals the
+ * same build run alone through the session API. */
+typedef struct OcpiJob {
+    const uint8_t* cloud;      /* host records; must stay valid until the job completes */
+    uint32_t pointAmount;
+    uint32_t dataStride;
+    uint8_t cloudType;         /* 0 float32, 1 float64 */
+    double scale[3];
+    double bbMin[3];           /* cubic bounding box; all six zero: computed on the device */
+    double bbMax[3];
+    uint32_t chunkingGrid;
+    uint32_t mergingThreshold;
+    float outputFactor;
+    uint32_t subsamplingGrid;
+    uint32_t modeFlags;        /* OCPI_SUB_* bits */
+    uint64_t seed;             /* explicit-random seed */
+    uint8_t* outRecords;       /* optional host array for octree.bin (see ocpi_set_output_host) */
+    uint32_t* outLut;          /* optional */
+    uint64_t outCapacity;      /* records */
+    uint8_t* outHierarchy;     /* optional host array for hierarchy.bin */
+    uint64_t outHierarchyCapacity;   /* bytes */
+} OcpiJob;
+
+typedef struct OcpiJobResult {
+    int32_t status;            /* 0 = built, -1 = failed (error holds the message) */
+    uint32_t lane;
+    uint32_t nodeCount;        /* hierarchy.bin entries */
+    uint64_t pointsTotal;      /* octree.bin records */
+    double queuedMs;           /* submission to start */
+    double runMs;              /* start to completion (upload, build, read-back) */
+    double totalMs;            /* submission to completion */
+    double deviceMs;           /* build stages, CUDA events */
+    char error[128];
+} OcpiJobResult;
+
+OCPI_EXPORT int ocpi_server_create(void** server, int device, uint32_t lanes, uint64_t memoryBudget);
+/* waits for the jobs in progress */
+OCPI_EXPORT int ocpi_server_destroy(void* server);
+OCPI_EXPORT int ocpi_server_submit(void* server, const OcpiJob* job, uint64_t* ticket);
+/* blocks until the job completes */
+OCPI_EXPORT int ocpi_server_wait(void* server, uint64_t ticket, OcpiJobResult* result);
+OCPI_EXPORT int ocpi_server_get_hierarchy(void* server, uint64_t ticket, uint8_t* out);
+/* forgets a completed job (waits for it first) */
+OCPI_EXPORT int ocpi_server_release(void* server, uint64_t ticket);
+/* all jobs submitted at once to a temporary executor; returns -1 if any failed */
+OCPI_EXPORT int ocpi_batch_build(int device, uint32_t lanes, uint64_t memoryBudget, const OcpiJob* jobs,
+                                 uint32_t count, OcpiJobResult* results);
+
 /* ---- allocation-free node subsampling (no counterpart in the reference) --
  *
  * For callers that may not allocate device memory: a plug-in living inside an

@@ -125,6 +125,29 @@ Builder::Builder(const BuildConfig& cfg, const uint8_t* host_cloud, int device) 
     check_cuda(cudaSetDevice(device_), "cudaSetDevice");
     check_cuda(cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, device_), "device attribute");
     check_cuda(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "stream");
+    check_cuda(cudaStreamCreateWithFlags(&side_stream_, cudaStreamNonBlocking), "stream");
+    check_cuda(cudaEventCreateWithFlags(&tree_ready_, cudaEventDisableTiming), "event");
+    size_for_config();
+    upload(host_cloud);
+}
+
+// A new cloud and configuration on the same device state: every buffer only
+// grows, so a builder that has served larger builds allocates nothing.
+void Builder::reconfigure(const BuildConfig& cfg, const uint8_t* host_cloud) {
+    cfg.validate();
+    if (copy_stream_) check_cuda(cudaStreamSynchronize(copy_stream_), "output copies");
+    cfg_ = cfg;
+    host_rec_ = nullptr;
+    host_lut_ = nullptr;
+    host_cap_ = 0;
+    host_filled_ = false;
+    nodes_.clear();
+    stats_ = Stats{};
+    size_for_config();
+    upload(host_cloud);
+}
+
+void Builder::size_for_config() {
     depth_ = ilog2(cfg_.chunk_grid);
     level_off_.assign(depth_ + 2, 0);
     for (uint32_t l = 0; l <= depth_; ++l) {
@@ -151,8 +174,6 @@ Builder::Builder(const BuildConfig& cfg, const uint8_t* host_cloud, int device) 
     child_first_.ensure((size_t)node_cap_ * 4);
     data_idx_.ensure((size_t)node_cap_ * 8);
     fill_.ensure((size_t)node_cap_ * 4);
-    check_cuda(cudaStreamCreateWithFlags(&side_stream_, cudaStreamNonBlocking), "stream");
-    check_cuda(cudaEventCreateWithFlags(&tree_ready_, cudaEventDisableTiming), "event");
     level_start_.ensure((depth_ + 2) * 4);
     n_nodes_.ensure(4);
     if (cfg_.has_bbox()) build_cell_tables();
@@ -160,7 +181,6 @@ Builder::Builder(const BuildConfig& cfg, const uint8_t* host_cloud, int device) 
     lut_.ensure((size_t)cfg_.n * 4);
     rec_.ensure((size_t)cfg_.n * 18 + 16);   // 16 readable bytes past the last record
     leaf_frac_.ensure((size_t)cfg_.n * 4);
-    upload(host_cloud);
 }
 
 // Exact boundary keys of the chunking grid for the current bounding box, and
@@ -283,12 +303,14 @@ std::vector<std::pair<std::string, uint64_t>> Builder::device_allocations() cons
 // Mirrors the sizing in Builder::Builder, generate() and subsample():
 // data-dependent buffers at their capacity rules (node capacity, staging and
 // final records at max(outputFactor * N, N), scratch at the staging capacity).
-uint64_t estimate_device_bytes(const BuildConfig& c, int num_sms) {
+// Every buffer's size is non-decreasing in each term, so the envelope of two
+// term sets bounds a builder that was reconfigured from one to the other.
+MemoryTerms memory_terms(const BuildConfig& c, int num_sms) {
+    MemoryTerms t;
     const uint32_t depth = ilog2(c.chunk_grid);
-    uint64_t cells = 0;
     for (uint32_t l = 0; l <= depth; ++l) {
         const uint64_t g = c.chunk_grid >> l;
-        cells += g * g * g;
+        t.cells += g * g * g;
     }
     uint64_t cap = 1;
     const uint64_t per = c.n / std::max<uint32_t>(c.threshold, 1);
@@ -296,29 +318,61 @@ uint64_t estimate_device_bytes(const BuildConfig& c, int num_sms) {
         const uint64_t g = c.chunk_grid >> l;
         cap += 8 * std::min<uint64_t>(g * g * g, per);
     }
-    const uint64_t node_cap = std::min<uint64_t>(cap, cells);
-    const uint64_t out_cap = std::max<uint64_t>((uint64_t)((float)c.n * c.output_factor), c.n);
+    t.node_cap = std::min<uint64_t>(cap, t.cells);
+    t.out_cap = std::max<uint64_t>((uint64_t)((float)c.n * c.output_factor), c.n);
+    t.n = c.n;
+    t.cloud_bytes = (uint64_t)c.n * c.stride;
+    t.chunk_grid = c.chunk_grid;
     const bool intra = c.intra, inter = !intra && c.inter, weighted = inter && c.weighting;
-    uint64_t per_cand = 4 + 8 + 4;                      // key cache, selection key, cell list
-    if (c.random) per_cand += 4;                        // selected candidate
-    if ((intra || inter) && !weighted) per_cand += 8;   // packed colour sums
-    if (weighted) per_cand += 12 + 4 + 4 + 20;          // cell units, cell groups
+    t.random = c.random;
+    t.packed = (intra || inter) && !weighted;
+    t.weighted = weighted;
     const uint64_t bs = (c.sub_grid + 3) / 4;
-    const uint64_t bricks = std::min<uint64_t>(out_cap, bs * bs * bs);
-    uint64_t slots = 1024;
-    while (slots * 11 / 16 < bricks + 1) slots <<= 1;
+    const uint64_t bricks = std::min<uint64_t>(t.out_cap, bs * bs * bs);
+    t.slots = 1024;
+    while (t.slots * 11 / 16 < bricks + 1) t.slots <<= 1;
+    t.sms = std::max(num_sms, 1);
+    return t;
+}
+
+MemoryTerms envelope(const MemoryTerms& a, const MemoryTerms& b) {
+    MemoryTerms t;
+    t.cloud_bytes = std::max(a.cloud_bytes, b.cloud_bytes);
+    t.n = std::max(a.n, b.n);
+    t.cells = std::max(a.cells, b.cells);
+    t.node_cap = std::max(a.node_cap, b.node_cap);
+    t.out_cap = std::max(a.out_cap, b.out_cap);
+    t.slots = std::max(a.slots, b.slots);
+    t.chunk_grid = std::max(a.chunk_grid, b.chunk_grid);
+    t.random = a.random || b.random;
+    t.packed = a.packed || b.packed;
+    t.weighted = a.weighted || b.weighted;
+    t.sms = std::max(a.sms, b.sms);
+    return t;
+}
+
+uint64_t device_bytes(const MemoryTerms& t) {
+    if (!t.n) return 0;
+    uint64_t per_cand = 4 + 8 + 4;       // key cache, selection key, cell list
+    if (t.random) per_cand += 4;         // selected candidate
+    if (t.packed) per_cand += 8;         // packed colour sums
+    if (t.weighted) per_cand += 12 + 4 + 4 + 20;   // cell units, cell groups
     uint64_t b = 0;
-    b += (uint64_t)c.n * c.stride + 64;                               // cloud
-    b += cells * 4;                                                    // count pyramid
-    b += node_cap * (4 + 4 + 1 + 2 + 4 + 4 + 8 + 4);                   // node table, leaf lists, fill
-    b += out_cap * (4 + 18) + 16;                                      // final LUT + records
-    b += out_cap * (4 + 18 + 4) + 64;                                  // staged LUT + records + sub-step words
-    b += (uint64_t)c.n * 4;                                            // leaf sub-step words
-    b += out_cap * per_cand;                                           // subsampling scratch
-    b += (uint64_t)std::max(num_sms, 1) * slots * 16;                  // per-block brick tables
-    b += node_cap * (sizeof(SubNode) + 4 + 8 + 4 + 8 + 8 + 8 + 4);     // level tables, placement lists
-    b += 3 * (c.chunk_grid + 2) * 8 + c.chunk_grid * 4 + 64 * 256;    // keys, spread, small buffers
+    b += t.cloud_bytes + 64;                                           // cloud
+    b += t.cells * 4;                                                  // count pyramid
+    b += t.node_cap * (4 + 4 + 1 + 2 + 4 + 4 + 8 + 4);                 // node table, leaf lists, fill
+    b += t.out_cap * (4 + 18) + 16;                                    // final LUT + records
+    b += t.out_cap * (4 + 18 + 4) + 64;                                // staged LUT + records + sub-step words
+    b += t.n * 4;                                                      // leaf sub-step words
+    b += t.out_cap * per_cand;                                         // subsampling scratch
+    b += (uint64_t)t.sms * t.slots * 16;                               // per-block brick tables
+    b += t.node_cap * (sizeof(SubNode) + 4 + 8 + 4 + 8 + 8 + 8 + 4);   // level tables, placement lists
+    b += 3 * (t.chunk_grid + 2) * 8 + t.chunk_grid * 4 + 64 * 256;    // keys, spread, small buffers
     return b;
+}
+
+uint64_t estimate_device_bytes(const BuildConfig& c, int num_sms) {
+    return device_bytes(memory_terms(c, num_sms));
 }
 
 // tools/memory_consumption.py:30-75 (countingGrid + denseToSparseLUT +

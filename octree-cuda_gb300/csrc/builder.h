@@ -91,6 +91,19 @@ struct Stats {
 uint64_t estimate_device_bytes(const BuildConfig& cfg, int num_sms);
 uint64_t reference_estimate_bytes(const BuildConfig& cfg);
 
+// The quantities the device buffers are sized from.  A builder reconfigured
+// through several configurations (its buffers only grow) stays within
+// device_bytes of the envelope of their terms.
+struct MemoryTerms {
+    uint64_t cloud_bytes = 0, n = 0, cells = 0, node_cap = 0, out_cap = 0, slots = 0;
+    uint32_t chunk_grid = 0;
+    bool random = false, packed = false, weighted = false;
+    int sms = 0;
+};
+MemoryTerms memory_terms(const BuildConfig& cfg, int num_sms);
+MemoryTerms envelope(const MemoryTerms& a, const MemoryTerms& b);
+uint64_t device_bytes(const MemoryTerms& t);
+
 class Builder {
 public:
     Builder(const BuildConfig& cfg, const uint8_t* host_cloud, int device);
@@ -100,6 +113,8 @@ public:
 
     // Uploads a new cloud of the same configuration (reuses allocations).
     void upload(const uint8_t* host_cloud);
+    // A new configuration and cloud; buffers only grow (see size_for_config).
+    void reconfigure(const BuildConfig& cfg, const uint8_t* host_cloud);
     void generate();
     // Real and cubic bounding boxes {minX, minY, minZ, maxX, maxY, maxZ} of
     // the uploaded cloud; the cubic box becomes the build's bounding box.
@@ -133,6 +148,7 @@ private:
     void check_device_errors(const char* stage);
     void build_tree_host();
     void build_cell_tables();
+    void size_for_config();
     void subsample();
     void compute_stats();
 

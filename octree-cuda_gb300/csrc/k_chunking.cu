@@ -13,7 +13,10 @@
 #include <algorithm>
 #include <climits>
 #include <cstdint>
+#include <map>
+#include <mutex>
 #include <type_traits>
+#include <utility>
 
 #include "device_common.cuh"
 #include "kernels.h"
@@ -680,9 +683,21 @@ __global__ void k_place_lut(const uint64_t* __restrict__ src_off, const uint64_t
 
 }   // namespace
 
+void allow_dynamic_smem(const void* kernel, size_t bytes) {
+    static std::mutex mu;
+    static std::map<std::pair<int, const void*>, size_t> limit;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> g(mu);
+    size_t& cur = limit[{dev, kernel}];
+    if (bytes <= cur) return;
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) == cudaSuccess) cur = bytes;
+    else cudaGetLastError();   // the launch reports the error
+}
+
 template <class Kernel>
 static int chunk_grid_size(Kernel kernel, uint32_t threads, uint32_t tile, size_t smem, uint64_t n, int num_sms) {
-    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    allow_dynamic_smem(reinterpret_cast<const void*>(kernel), smem);
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess || per_sm < 1)
         per_sm = 1;

@@ -753,7 +753,7 @@ void launch_one(const SubLevelArgs& a, int num_sms, size_t smem, cudaStream_t st
     const uint32_t cs = kCanCluster ? cluster_size(a.n_nodes, num_sms) : 1u;
     if (cs > 1) {
         auto kern = k_subsample<kF32, kColor, kRandom, kCanCluster>;
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        allow_dynamic_smem(reinterpret_cast<const void*>(kern), smem);
         cudaLaunchConfig_t cfg = {};
         cudaLaunchAttribute attr[1];
         attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -775,7 +775,7 @@ void launch_one(const SubLevelArgs& a, int num_sms, size_t smem, cudaStream_t st
         cudaGetLastError();   // no cluster of this size fits: one block per node
     }
     auto kern = k_subsample<kF32, kColor, kRandom, false>;
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    allow_dynamic_smem(reinterpret_cast<const void*>(kern), smem);
     const int grid = (int)std::min<uint32_t>(a.n_nodes, (uint32_t)num_sms);
     kern<<<grid, kSubThreads, smem, stream>>>(a);
 }

@@ -173,6 +173,11 @@ size_t subsample_smem_bytes();
 uint32_t subsample_block_size();
 int launch_subsample_level(const SubLevelArgs& a, int num_sms, cudaStream_t stream);
 
+// Raises a kernel's dynamic shared memory limit on the current device to at
+// least `bytes` and never lowers it, so that builders launching the same
+// kernel from several host threads cannot undercut each other's launches.
+void allow_dynamic_smem(const void* kernel, size_t bytes);
+
 // Moves staged internal-node records to their final (post-order) positions.
 int launch_place(const uint64_t* src_off, const uint64_t* dst_off, const uint32_t* count, uint32_t n_nodes,
                  const uint8_t* stage_rec, uint8_t* rec, cudaStream_t stream);

@@ -210,7 +210,12 @@ int ocpi_init_octree(void* session) {
             s->builder->upload(s->host_cloud);   // same configuration: reuse device state
             return;
         }
-        s->builder.reset();
+        if (s->builder) {
+            // another configuration: the same buffers, grown where needed
+            s->builder->reconfigure(s->cfg, s->host_cloud);
+            if (s->out_rec) s->builder->set_output_host(s->out_rec, s->out_lut, s->out_cap);
+            return;
+        }
         s->builder = std::make_unique<oc::Builder>(s->cfg, s->host_cloud, s->device);
         cudaDeviceGetAttribute(&s->builder_sms, cudaDevAttrMultiProcessorCount, s->device);
         if (s->out_rec) s->builder->set_output_host(s->out_rec, s->out_lut, s->out_cap);

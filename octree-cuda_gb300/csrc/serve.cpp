@@ -1,0 +1,376 @@
+// Batched and served forms of the LOD build: an executor that runs many
+// independent builds at once on one GPU.
+//
+// Each of `lanes` worker threads owns one Builder (its own streams and
+// buffers).  A lane reconfigures its builder for every job, so after the
+// first few jobs its buffers have grown to the sizes in use and it
+// allocates nothing more: no cudaFree, which would stall every other lane.
+// While one lane waits on its host steps (tree read-back, level
+// bookkeeping, the final read-back), the others keep the GPU busy.
+//
+// Admission: a job's device memory is bounded by estimate_device_bytes.  A
+// lane reserves the bound of the envelope of the jobs its builder has run
+// (buffers only grow, each to the largest size any of those jobs needed); a
+// job starts on a free lane only while the sum of the reservations, with that
+// lane's envelope widened by the job, stays within the executor's budget.
+// Among the waiting jobs the oldest that fits is taken first; a job whose
+// bound exceeds the budget alone fails at submission.  An idle lane whose
+// memory keeps a waiting job out frees its builder.
+//
+// Results do not depend on the mix: each build owns its state, and every
+// kernel is deterministic up to the order of records inside a node.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/octreeApi.h"
+#include "builder.h"
+
+namespace oc {
+
+void set_last_error(const std::string& msg);
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+double ms_between(Clock::time_point a, Clock::time_point b) {
+    return std::chrono::duration<double, std::milli>(b - a).count();
+}
+
+struct Job {
+    uint64_t ticket = 0;
+    OcpiJob spec{};
+    BuildConfig cfg;
+    MemoryTerms terms;
+    uint64_t bound = 0;   // device bytes (estimate_device_bytes)
+    Clock::time_point submitted, started, finished;
+    bool done = false;
+    OcpiJobResult result{};
+    std::vector<uint8_t> hierarchy;
+};
+
+BuildConfig config_of(const OcpiJob& j) {
+    BuildConfig c;
+    c.n = j.pointAmount;
+    c.stride = j.dataStride;
+    c.cloud_type = j.cloudType;
+    for (int a = 0; a < 3; ++a) {
+        c.scale[a] = j.scale[a];
+        c.offset[a] = j.bbMin[a];
+        c.bb_min[a] = j.bbMin[a];
+        c.bb_max[a] = j.bbMax[a];
+    }
+    c.chunk_grid = j.chunkingGrid;
+    c.threshold = j.mergingThreshold;
+    c.output_factor = j.outputFactor;
+    c.sub_grid = j.subsamplingGrid;
+    c.intra = (j.modeFlags & OCPI_SUB_INTRA) != 0;
+    c.inter = (j.modeFlags & OCPI_SUB_INTER) != 0;
+    c.replacement = true;
+    c.random = (j.modeFlags & OCPI_SUB_RANDOM) != 0;
+    c.weighting = (j.modeFlags & OCPI_SUB_WEIGHTING) != 0;
+    c.seed = j.seed;
+    return c;
+}
+
+class Executor {
+public:
+    Executor(int device, uint32_t lanes, uint64_t budget) : device_(device), budget_(budget) {
+        check_cuda(cudaSetDevice(device), "cudaSetDevice");
+        check_cuda(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, device), "device attribute");
+        reserved_.assign(lanes, 0);
+        env_.assign(lanes, MemoryTerms{});
+        busy_.assign(lanes, false);
+        releasing_.assign(lanes, false);
+        for (uint32_t l = 0; l < lanes; ++l) workers_.emplace_back([this, l] { run_lane(l); });
+    }
+
+    // Jobs in progress complete; jobs still waiting fail.
+    ~Executor() {
+        {
+            std::lock_guard<std::mutex> g(mu_);
+            stop_ = true;
+            for (auto& job : queue_) {
+                job->result.status = -1;
+                std::snprintf(job->result.error, sizeof job->result.error, "server destroyed before the job started");
+                job->done = true;
+            }
+            queue_.clear();
+        }
+        cv_work_.notify_all();
+        cv_done_.notify_all();
+        for (auto& t : workers_) t.join();
+    }
+
+    uint64_t submit(const OcpiJob& spec) {
+        auto job = std::make_shared<Job>();
+        job->spec = spec;
+        job->cfg = config_of(spec);
+        job->cfg.validate();
+        if (!spec.cloud) throw Error("job without a point cloud");
+        job->terms = memory_terms(job->cfg, sms_);
+        job->bound = device_bytes(job->terms);
+        if (job->bound > budget_)
+            throw Error("job needs up to " + std::to_string(job->bound) + " device bytes, above the executor budget of " +
+                        std::to_string(budget_));
+        std::lock_guard<std::mutex> g(mu_);
+        job->ticket = ++next_ticket_;
+        job->submitted = Clock::now();
+        jobs_[job->ticket] = job;
+        queue_.push_back(job);
+        cv_work_.notify_all();
+        return job->ticket;
+    }
+
+    OcpiJobResult wait(uint64_t ticket) {
+        std::unique_lock<std::mutex> g(mu_);
+        auto it = jobs_.find(ticket);
+        if (it == jobs_.end()) throw Error("unknown ticket");
+        auto job = it->second;
+        cv_done_.wait(g, [&] { return job->done; });
+        return job->result;
+    }
+
+    void hierarchy(uint64_t ticket, uint8_t* out) {
+        std::unique_lock<std::mutex> g(mu_);
+        auto it = jobs_.find(ticket);
+        if (it == jobs_.end()) throw Error("unknown ticket");
+        auto job = it->second;
+        cv_done_.wait(g, [&] { return job->done; });
+        std::memcpy(out, job->hierarchy.data(), job->hierarchy.size());
+    }
+
+    void release(uint64_t ticket) {
+        std::unique_lock<std::mutex> g(mu_);
+        auto it = jobs_.find(ticket);
+        if (it == jobs_.end()) throw Error("unknown ticket");
+        auto job = it->second;
+        cv_done_.wait(g, [&] { return job->done; });
+        jobs_.erase(it);
+    }
+
+private:
+    // The oldest waiting job that fits the budget on lane l (mutex held).
+    std::shared_ptr<Job> take(uint32_t l) {
+        uint64_t others = 0;
+        for (size_t k = 0; k < reserved_.size(); ++k)
+            if (k != l) others += reserved_[k];
+        for (auto it = queue_.begin(); it != queue_.end(); ++it) {
+            const MemoryTerms env = envelope(env_[l], (*it)->terms);
+            const uint64_t mine = device_bytes(env);
+            if (others + mine <= budget_) {
+                auto job = *it;
+                queue_.erase(it);
+                env_[l] = env;
+                reserved_[l] = mine;
+                return job;
+            }
+        }
+        return nullptr;
+    }
+
+    // True when idle lane l should give its memory back to a waiting job
+    // (mutex held): the job fits once this lane's memory is freed, or only
+    // once every idle lane's is (then all of them free it).  Memory of lanes
+    // already freeing theirs counts as free here, not in take().
+    bool blocked_by(uint32_t l) const {
+        if (queue_.empty() || reserved_[l] == 0 || releasing_[l]) return false;
+        uint64_t others = 0, busy = 0;
+        for (size_t k = 0; k < reserved_.size(); ++k) {
+            if (k == l || releasing_[k]) continue;
+            others += reserved_[k];
+            if (busy_[k]) busy += reserved_[k];
+        }
+        for (const auto& j : queue_)
+            if (others + j->bound <= budget_) return true;
+        for (const auto& j : queue_)
+            if (busy + j->bound <= budget_) return true;
+        return false;
+    }
+
+    void run_lane(uint32_t l) {
+        cudaSetDevice(device_);
+        std::unique_ptr<Builder> builder;
+        for (;;) {
+            std::shared_ptr<Job> job;
+            bool shrink = false;
+            {
+                std::unique_lock<std::mutex> g(mu_);
+                cv_work_.wait(g, [&] {
+                    if (stop_) return true;
+                    job = take(l);
+                    if (job) return true;
+                    shrink = blocked_by(l);   // idle and holding memory a waiting job needs
+                    return shrink;
+                });
+                if (!job && !shrink) return;   // stopping
+                if (shrink) releasing_[l] = true;
+                if (job) {
+                    busy_[l] = true;
+                    job->started = Clock::now();
+                }
+            }
+            if (!job) {
+                builder.reset();   // frees this lane's buffers
+                {
+                    std::lock_guard<std::mutex> g(mu_);
+                    reserved_[l] = 0;
+                    env_[l] = MemoryTerms{};
+                    releasing_[l] = false;
+                }
+                cv_work_.notify_all();
+                continue;
+            }
+            OcpiJobResult r{};
+            std::vector<uint8_t> hier;
+            try {
+                const OcpiJob& s = job->spec;
+                BuildConfig cfg = job->cfg;
+                const bool device_bb = !cfg.has_bbox();
+                if (!builder) builder = std::make_unique<Builder>(cfg, s.cloud, device_);
+                else builder->reconfigure(cfg, s.cloud);
+                if (device_bb) {
+                    double real[6], cubic[6];
+                    builder->compute_bbox(real, cubic);
+                }
+                if (s.outRecords) builder->set_output_host(s.outRecords, s.outLut, s.outCapacity);
+                builder->generate();
+                hier = builder->hierarchy();
+                if (s.outHierarchy) {
+                    if (hier.size() > s.outHierarchyCapacity)
+                        throw Error("hierarchy output too small: the octree has " + std::to_string(hier.size() / 22) +
+                                    " nodes");
+                    std::memcpy(s.outHierarchy, hier.data(), hier.size());
+                }
+                const Stats& st = builder->stats();
+                r.status = 0;
+                r.nodeCount = st.tree_nodes;
+                r.pointsTotal = st.points_total;
+                for (const auto& t : builder->timings()) r.deviceMs += t.second;
+            } catch (const std::exception& e) {
+                r.status = -1;
+                std::snprintf(r.error, sizeof r.error, "%s", e.what());
+                builder.reset();   // leave no half-finished device state behind
+                cudaGetLastError();
+            }
+            {
+                std::lock_guard<std::mutex> g(mu_);
+                job->finished = Clock::now();
+                r.queuedMs = ms_between(job->submitted, job->started);
+                r.runMs = ms_between(job->started, job->finished);
+                r.totalMs = ms_between(job->submitted, job->finished);
+                r.lane = l;
+                job->result = r;
+                job->hierarchy = std::move(hier);
+                job->done = true;
+                busy_[l] = false;
+                if (!builder) {
+                    reserved_[l] = 0;
+                    env_[l] = MemoryTerms{};
+                }
+            }
+            cv_done_.notify_all();
+            cv_work_.notify_all();   // a reservation may have changed
+        }
+    }
+
+    int device_;
+    int sms_ = 152;
+    uint64_t budget_;
+    std::mutex mu_;
+    std::condition_variable cv_work_, cv_done_;
+    std::deque<std::shared_ptr<Job>> queue_;
+    std::map<uint64_t, std::shared_ptr<Job>> jobs_;
+    std::vector<uint64_t> reserved_;   // device bytes held or claimed per lane
+    std::vector<MemoryTerms> env_;     // envelope of the jobs each lane's builder has run
+    std::vector<bool> busy_, releasing_;
+    std::vector<std::thread> workers_;
+    uint64_t next_ticket_ = 0;
+    bool stop_ = false;
+};
+
+template <class F>
+int guarded(F&& fn) {
+    try {
+        fn();
+        return SUCCESS;
+    } catch (const std::exception& e) {
+        set_last_error(e.what());
+        return UNEXPECTED_ERROR;
+    }
+}
+
+Executor* to_executor(void* p) {
+    if (!p) throw Error("null executor");
+    return static_cast<Executor*>(p);
+}
+
+}   // namespace
+}   // namespace oc
+
+extern "C" {
+
+int ocpi_server_create(void** server, int device, uint32_t lanes, uint64_t memoryBudget) {
+    return oc::guarded([&] {
+        if (!server) throw oc::Error("null server pointer");
+        if (lanes < 1 || lanes > 64) throw oc::Error("lanes must be in [1, 64]");
+        *server = new oc::Executor(device, lanes, memoryBudget);
+    });
+}
+
+int ocpi_server_destroy(void* server) {
+    return oc::guarded([&] { delete oc::to_executor(server); });
+}
+
+int ocpi_server_submit(void* server, const OcpiJob* job, uint64_t* ticket) {
+    return oc::guarded([&] {
+        if (!job || !ticket) throw oc::Error("null argument");
+        *ticket = oc::to_executor(server)->submit(*job);
+    });
+}
+
+int ocpi_server_wait(void* server, uint64_t ticket, OcpiJobResult* result) {
+    return oc::guarded([&] {
+        const OcpiJobResult r = oc::to_executor(server)->wait(ticket);
+        if (result) *result = r;
+    });
+}
+
+int ocpi_server_get_hierarchy(void* server, uint64_t ticket, uint8_t* out) {
+    return oc::guarded([&] {
+        if (!out) throw oc::Error("null output");
+        oc::to_executor(server)->hierarchy(ticket, out);
+    });
+}
+
+int ocpi_server_release(void* server, uint64_t ticket) {
+    return oc::guarded([&] { oc::to_executor(server)->release(ticket); });
+}
+
+int ocpi_batch_build(int device, uint32_t lanes, uint64_t memoryBudget, const OcpiJob* jobs, uint32_t count,
+                     OcpiJobResult* results) {
+    return oc::guarded([&] {
+        if (!jobs || !results) throw oc::Error("null argument");
+        oc::Executor ex(device, lanes, memoryBudget);
+        std::vector<uint64_t> tickets(count);
+        for (uint32_t i = 0; i < count; ++i) tickets[i] = ex.submit(jobs[i]);
+        bool ok = true;
+        for (uint32_t i = 0; i < count; ++i) {
+            results[i] = ex.wait(tickets[i]);
+            ok = ok && results[i].status == 0;
+        }
+        if (!ok) throw oc::Error("some builds of the batch failed (see their results)");
+    });
+}
+
+}   // extern "C"

@@ -31,6 +31,8 @@ ADDED_SYMBOLS = [
     "ocpi_get_node_count", "ocpi_get_hierarchy", "ocpi_get_records", "ocpi_get_lut",
     "ocpi_get_level_counts", "ocpi_get_timings", "ocpi_subsample_node_noalloc", "ocpi_set_output_host",
     "ocpi_compute_cloud_bb", "ocpi_get_device_memory", "ocpi_estimate_memory",
+    "ocpi_server_create", "ocpi_server_destroy", "ocpi_server_submit", "ocpi_server_wait",
+    "ocpi_server_get_hierarchy", "ocpi_server_release", "ocpi_batch_build",
 ]
 
 HIER_DTYPE = np.dtype([("type", "u1"), ("mask", "u1"), ("points", "<u4"),
@@ -60,6 +62,25 @@ class OcpiStats(ctypes.Structure):
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_ if n != "reserved"}
+
+
+class OcpiJob(ctypes.Structure):
+    _fields_ = [
+        ("cloud", ctypes.c_void_p), ("pointAmount", ctypes.c_uint32), ("dataStride", ctypes.c_uint32),
+        ("cloudType", ctypes.c_uint8), ("scale", ctypes.c_double * 3), ("bbMin", ctypes.c_double * 3),
+        ("bbMax", ctypes.c_double * 3), ("chunkingGrid", ctypes.c_uint32), ("mergingThreshold", ctypes.c_uint32),
+        ("outputFactor", ctypes.c_float), ("subsamplingGrid", ctypes.c_uint32), ("modeFlags", ctypes.c_uint32),
+        ("seed", ctypes.c_uint64), ("outRecords", ctypes.c_void_p), ("outLut", ctypes.c_void_p),
+        ("outCapacity", ctypes.c_uint64), ("outHierarchy", ctypes.c_void_p), ("outHierarchyCapacity", ctypes.c_uint64),
+    ]
+
+
+class OcpiJobResult(ctypes.Structure):
+    _fields_ = [
+        ("status", ctypes.c_int32), ("lane", ctypes.c_uint32), ("nodeCount", ctypes.c_uint32),
+        ("pointsTotal", ctypes.c_uint64), ("queuedMs", ctypes.c_double), ("runMs", ctypes.c_double),
+        ("totalMs", ctypes.c_double), ("deviceMs", ctypes.c_double), ("error", ctypes.c_char * 128),
+    ]
 
 
 _lib = None
@@ -108,6 +129,13 @@ def load_library(path=LIB_PATH):
         "ocpi_set_output_host": [vp, vp, vp, u64],
         "ocpi_compute_cloud_bb": [vp, vp, vp],
         "ocpi_get_device_memory": [vp, ctypes.POINTER(u64)],
+        "ocpi_server_create": [ctypes.POINTER(vp), ctypes.c_int, u32, u64],
+        "ocpi_server_destroy": [vp],
+        "ocpi_server_submit": [vp, ctypes.POINTER(OcpiJob), ctypes.POINTER(u64)],
+        "ocpi_server_wait": [vp, u64, ctypes.POINTER(OcpiJobResult)],
+        "ocpi_server_get_hierarchy": [vp, u64, vp],
+        "ocpi_server_release": [vp, u64],
+        "ocpi_batch_build": [ctypes.c_int, u32, u64, ctypes.POINTER(OcpiJob), u32, ctypes.POINTER(OcpiJobResult)],
         "ocpi_estimate_memory": [u32, u32, u8, u32, u32, ctypes.c_float, u32, u32, ctypes.POINTER(u64),
                                  ctypes.POINTER(u64)],
         "ocpi_subsample_node_noalloc": [vp, u8, u32, ctypes.POINTER(d), ctypes.POINTER(d), ctypes.POINTER(d), d,
@@ -318,3 +346,75 @@ def build_octree(cloud, *, n, stride, cloud_type, scale, bb_min, bb_max, device=
     s.init()
     s.generate()
     return s, s.stats()
+
+
+def make_job(cloud, *, n, stride, cloud_type, scale, bb_min=None, bb_max=None, chunk_grid=512, merge_threshold=10000,
+             output_factor=2.2, sub_grid=128, flags=SUB_INTER, seed=0x5EED, records=None, lut=None, hierarchy=None):
+    """OcpiJob for Server.submit / batch_build.  bb_min None: the box is
+    computed on the device.  records / lut / hierarchy: optional host arrays
+    the build fills (keep them, and the cloud, alive until it completes)."""
+    j = OcpiJob()
+    j.cloud = cloud.ctypes.data
+    j.pointAmount, j.dataStride, j.cloudType = n, stride, cloud_type
+    j.scale[:] = [float(v) for v in scale]
+    if bb_min is not None:
+        j.bbMin[:] = [float(v) for v in bb_min]
+        j.bbMax[:] = [float(v) for v in bb_max]
+    j.chunkingGrid, j.mergingThreshold, j.outputFactor, j.subsamplingGrid = chunk_grid, merge_threshold, output_factor, sub_grid
+    j.modeFlags, j.seed = flags, seed
+    if records is not None:
+        j.outRecords, j.outCapacity = records.ctypes.data, len(records) // 18
+        j.outLut = lut.ctypes.data if lut is not None else None
+    if hierarchy is not None:
+        j.outHierarchy, j.outHierarchyCapacity = hierarchy.ctypes.data, len(hierarchy)
+    return j
+
+
+class Server:
+    """Executor of independent builds on one GPU (ocpi_server_*)."""
+
+    def __init__(self, device=0, lanes=4, memory_budget=150 << 30):
+        L = load_library()
+        h = ctypes.c_void_p()
+        _check(L.ocpi_server_create(ctypes.byref(h), device, lanes, memory_budget), "ocpi_server_create")
+        self._h = h
+
+    def submit(self, job):
+        t = ctypes.c_uint64()
+        _check(load_library().ocpi_server_submit(self._h, ctypes.byref(job), ctypes.byref(t)), "ocpi_server_submit")
+        return t.value
+
+    def wait(self, ticket):
+        r = OcpiJobResult()
+        _check(load_library().ocpi_server_wait(self._h, ticket, ctypes.byref(r)), "ocpi_server_wait")
+        return r
+
+    def hierarchy(self, ticket, node_count):
+        out = np.zeros(node_count, HIER_DTYPE)
+        _check(load_library().ocpi_server_get_hierarchy(self._h, ticket, out.ctypes.data), "ocpi_server_get_hierarchy")
+        return out
+
+    def release(self, ticket):
+        _check(load_library().ocpi_server_release(self._h, ticket), "ocpi_server_release")
+
+    def close(self):
+        if self._h:
+            load_library().ocpi_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def batch_build(jobs, device=0, lanes=4, memory_budget=150 << 30):
+    """Builds every job of a list at once; returns their OcpiJobResults
+    (per-build failures are reported there, not raised)."""
+    arr = (OcpiJob * len(jobs))(*jobs)
+    res = (OcpiJobResult * len(jobs))()
+    rc = load_library().ocpi_batch_build(device, lanes, memory_budget, arr, len(jobs), res)
+    if rc != 0 and all(r.status == 0 for r in res):
+        _check(rc, "ocpi_batch_build")   # rejected before any build ran
+    return list(res)   # a failed build has status -1 and its message in .error

@@ -1,0 +1,89 @@
+"""Batched and served forms (ocpi_batch_build, ocpi_server_*): every build
+run in the mix equals the same build run alone through the session API --
+hierarchy.bin byte-identical, each node's records equal as a multiset."""
+import numpy as np
+import pytest
+
+from helpers import make_case, node_sorted, octree_api, run_gpu
+
+pytestmark = pytest.mark.gpu
+
+MODES = [dict(inter=True), dict(random=True, intra=True), dict(random=True, inter=True, weighting=True), dict()]
+FLAGS = [octree_api.SUB_INTER, octree_api.SUB_RANDOM | octree_api.SUB_INTRA,
+         octree_api.SUB_RANDOM | octree_api.SUB_INTER | octree_api.SUB_WEIGHTING, 0]
+
+
+def mixed_cases(count):
+    rng = np.random.default_rng(7)
+    out = []
+    for i in range(count):
+        n = int(np.exp(rng.uniform(np.log(20_000), np.log(400_000))))
+        cloud_type = 0 if rng.random() < 0.8 else 1
+        grids = (64, 32) if rng.random() < 0.5 else (128, 64)
+        m = int(rng.integers(len(MODES)))
+        out.append((make_case(i % 3, cloud_type, n, seed=1000 + i), grids, m))
+    return out
+
+
+def alone(case, grids, m):
+    cfg = dict(chunk_grid=grids[0], sub_grid=grids[1], merge_threshold=2000, seed=99, **MODES[m])
+    s = run_gpu(case, cfg)
+    h, r, l = s.hierarchy(), s.records(), s.lut()
+    s.close()
+    return h, r, l
+
+
+def job_for(case, grids, m, rec, lut, hier, device_bbox=False):
+    kw = {} if device_bbox else dict(bb_min=case.bb_min, bb_max=case.bb_max)
+    return octree_api.make_job(case.cloud, n=case.n, stride=case.stride, cloud_type=case.cloud_type, scale=case.scale,
+                               chunk_grid=grids[0], sub_grid=grids[1], merge_threshold=2000, flags=FLAGS[m], seed=99,
+                               records=rec, lut=lut, hierarchy=hier, **kw)
+
+
+def check_same(want, res, rec, lut, hier):
+    wh, wr, wl = want
+    assert res.status == 0, res.error
+    assert res.nodeCount == len(wh) and res.pointsTotal == len(wr)
+    got_h = hier[: res.nodeCount * 22].view(octree_api.HIER_DTYPE)
+    assert got_h.tobytes() == wh.tobytes(), "hierarchy differs from the build run alone"
+    got_r = rec[: res.pointsTotal * 18].view(octree_api.RECORD_DTYPE)
+    a_r, a_l = node_sorted(wh, wr, wl)
+    b_r, b_l = node_sorted(got_h, got_r, lut[: res.pointsTotal])
+    assert np.array_equal(a_l, b_l) and a_r.tobytes() == b_r.tobytes(), "records differ from the build run alone"
+
+
+def buffers(want):
+    """Host outputs holding exactly the records and nodes of the build."""
+    h, r, _ = want
+    return np.zeros(len(r) * 18, np.uint8), np.zeros(len(r), np.uint32), np.zeros(len(h) * 22, np.uint8)
+
+
+def test_batch_equals_builds_alone():
+    cases = mixed_cases(12)
+    want = [alone(c, g, m) for c, g, m in cases]
+    bufs = [buffers(w) for w in want]
+    jobs = [job_for(c, g, m, *b, device_bbox=(i % 4 == 0)) for i, ((c, g, m), b) in enumerate(zip(cases, bufs))]
+    results = octree_api.batch_build(jobs, lanes=4)
+    for w, r, b in zip(want, results, bufs):
+        check_same(w, r, *b)
+
+
+def test_server_admission_under_a_small_budget():
+    """A budget that holds about two builds at a time: jobs queue, every one
+    completes, results equal the builds alone; an oversized job is refused."""
+    cases = mixed_cases(8)
+    bounds = [octree_api.estimate_memory(c.n, c.stride, c.cloud_type, g[0], 2000, 2.2, g[1], FLAGS[m])[0]
+              for c, g, m in cases]
+    budget = int(2.2 * max(bounds))
+    want = [alone(c, g, m) for c, g, m in cases]
+    srv = octree_api.Server(lanes=4, memory_budget=budget)
+    bufs = [buffers(w) for w in want]
+    tickets = [srv.submit(job_for(c, g, m, *b)) for (c, g, m), b in zip(cases, bufs)]
+    results = [srv.wait(t) for t in tickets]
+    for w, r, b in zip(want, results, bufs):
+        check_same(w, r, *b)
+    assert max(r.queuedMs for r in results) > 0
+    big = make_case(0, 0, 2_000_000, seed=5)
+    with pytest.raises(octree_api.OctreeError, match="budget"):
+        srv.submit(job_for(big, (512, 128), 0, None, None, None))
+    srv.close()
