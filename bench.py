@@ -180,6 +180,310 @@ def run_reference_arm(args):
     return 0
 
 
+# ---------------------------------------------------------------- forms
+# Batched (256 independent clouds at once) and served (a Poisson stream of
+# build requests) forms through ocpi_batch_build / ocpi_server_*, each beside
+# the same builds run one at a time through the plain session calls.
+
+# per generator kind: subsampling options and scale of the plain workloads
+# (heightfield: implicit + inter, scale 0.001; planes and cylinders: explicit
+# random + inter + weighting, scale 0.001; Zipf terrain: inter, scale 0.01)
+KIND_MODES = {0: dict(inter=True), 1: dict(random=True, inter=True, weighting=True), 2: dict(inter=True)}
+KIND_SCALE = {0: float(np.float32(0.001)), 1: float(np.float32(0.001)), 2: float(np.float32(0.01))}
+FORM_SEED = 20240701
+
+
+def mode_flags(m):
+    import octree_api
+
+    return ((octree_api.SUB_INTRA if m.get("intra") else 0) | (octree_api.SUB_INTER if m.get("inter") else 0) |
+            (octree_api.SUB_RANDOM if m.get("random") else 0) | (octree_api.SUB_WEIGHTING if m.get("weighting") else 0))
+
+
+def host_memory_available():
+    try:
+        with open("/proc/meminfo") as f:
+            for ln in f:
+                if ln.startswith("MemAvailable:"):
+                    return int(ln.split()[1]) * 1024
+    except Exception:
+        pass
+    return None
+
+
+def check_host_memory(nbytes):
+    """Refuses a workload whose pinned buffers would take more than half of
+    the host memory still available."""
+    avail = host_memory_available()
+    if avail is not None and nbytes > avail // 2:
+        raise SystemExit("workload needs %.1f GB of pinned host memory, %.1f GB available: reduce it" %
+                         (nbytes / 1e9, avail / 1e9))
+
+
+class FormCloud:
+    """One seeded cloud of a form workload, held in pinned host memory."""
+
+    def __init__(self, i, kind, cloud_type, n, seed, threads):
+        import octree_api
+
+        self.i, self.kind, self.cloud_type, self.n, self.seed = i, kind, cloud_type, n, seed
+        self.stride = 15 if cloud_type == 0 else 27
+        c = octree_api.synthetic_cloud(kind, cloud_type, n, seed, self.stride, threads)
+        self.bb = octree_api.cubic_bbox(c, n, self.stride, cloud_type, threads)
+        self.host = pinned_bytes(c.nbytes)
+        self.host[:] = c
+        self.scale = KIND_SCALE[kind]
+
+
+def plain_build(s, c, grids, mode, rec, hier_out=None):
+    """One build through the plain session calls, results into host arrays;
+    returns (points_total, node count)."""
+    import octree_api
+
+    s.set_cloud(c.host, n=c.n, stride=c.stride, cloud_type=c.cloud_type, scale=[c.scale] * 3, bb_min=c.bb[:3],
+                bb_max=c.bb[3:])
+    s.configure(chunk_grid=grids[0], merge_threshold=10000, output_factor=2.2, sub_grid=grids[1], seed=c.seed, **mode)
+    if rec is not None:
+        s.set_output_host(rec)
+    s.init()
+    s.generate()
+    L = octree_api.load_library()
+    nodes = ctypes_u64()
+    octree_api._check(L.ocpi_get_node_count(s._h, nodes), "ocpi_get_node_count")
+    if hier_out is not None:
+        octree_api._check(L.ocpi_get_hierarchy(s._h, hier_out.ctypes.data), "ocpi_get_hierarchy")
+    if rec is not None:
+        octree_api._check(L.ocpi_get_records(s._h, rec.ctypes.data), "ocpi_get_records")
+    return s.stats()["points_total"], nodes.value
+
+
+def ctypes_u64():
+    import ctypes
+
+    return ctypes.c_uint64()
+
+
+def form_job(c, grids, mode, rec, hier):
+    import octree_api
+
+    return octree_api.make_job(c.host, n=c.n, stride=c.stride, cloud_type=c.cloud_type, scale=[c.scale] * 3,
+                               bb_min=c.bb[:3], bb_max=c.bb[3:], chunk_grid=grids[0], merge_threshold=10000,
+                               output_factor=2.2, sub_grid=grids[1], flags=mode_flags(mode), seed=c.seed,
+                               records=rec, hierarchy=hier)
+
+
+def form_line(args, metric, value, unit, extra):
+    line = {"metric": metric, "value": round(value, 3), "unit": unit, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32/f64", "data": "synthetic"}
+    line.update(extra)
+    return line
+
+
+def run_batched(args):
+    """256 clouds, sizes log-uniform 50k-4M (seeded), 80% float32, grids
+    128/64 or 512/128 at random, generators in turn; per-cloud seeds."""
+    import octree_api
+
+    threads = os.cpu_count() or 1
+    rng = np.random.default_rng(FORM_SEED)
+    count = args.clouds
+    sizes = np.exp(rng.uniform(np.log(50_000), np.log(4_000_000), count)).astype(np.int64)
+    types = (rng.random(count) >= 0.8).astype(int)
+    grid_pick = rng.random(count) < 0.5
+    t0 = time.time()
+    clouds = [FormCloud(i, i % 3, int(types[i]), int(sizes[i]), FORM_SEED + i, threads) for i in range(count)]
+    gen_s = time.time() - t0
+    grids = [(128, 64) if g else (512, 128) for g in grid_pick]
+    modes = [KIND_MODES[c.kind] for c in clouds]
+    total_pts = int(sizes.sum())
+
+    # output sizes from one plain pass (warm-up), then exact pinned outputs
+    s = octree_api.OctreeSession(0)
+    shapes = []
+    for c, g, m in zip(clouds, grids, modes):
+        shapes.append(plain_build(s, c, g, m, None))
+    need = sum(max(p, 1) * 18 for p, _ in shapes)
+    check_host_memory(need + sum(c.host.nbytes for c in clouds))
+    recs = [pinned_bytes(max(p, 1) * 18) for p, _ in shapes]
+    hiers = [np.zeros(nn * 22, np.uint8) for _, nn in shapes]
+    out_bytes = sum(p * 18 + nn * 22 for p, nn in shapes)
+    in_bytes = sum(c.n * c.stride for c in clouds)
+
+    def plain_pass():
+        t = time.perf_counter()
+        for c, g, m, r, h in zip(clouds, grids, modes, recs, hiers):
+            plain_build(s, c, g, m, r, h)
+        return time.perf_counter() - t
+
+    jobs = [form_job(c, g, m, r, h) for c, g, m, r, h in zip(clouds, grids, modes, recs, hiers)]
+
+    def batch_pass():
+        t = time.perf_counter()
+        res = octree_api.batch_build(jobs, lanes=args.lanes, memory_budget=args.budget_gb << 30)
+        dt = time.perf_counter() - t
+        bad = [r.error.decode() for r in res if r.status != 0]
+        if bad:
+            raise RuntimeError("batched build failed: %s" % bad[0])
+        return dt, res
+
+    for _ in range(max(1, args.warmup - 1)):
+        plain_pass()
+    plain_s = [plain_pass() for _ in range(args.steps)]
+    for _ in range(args.warmup):
+        batch_pass()
+    clocks = ClockSampler(0)
+    clocks.start()
+    batch = [batch_pass() for _ in range(args.steps)]
+    clk = clocks.stop()
+    s.close()
+    b_s = statistics.median(d for d, _ in batch)
+    p_s = statistics.median(plain_s)
+    res = batch[-1][1]
+    line = form_line(args, "Mpts/s batched build, %d clouds" % count, total_pts / b_s / 1e6, "Mpts/s", {
+        "form": "batched", "ms_per_step": round(b_s * 1e3, 2),
+        "config": {"workload": "batched_%d_clouds_50k_4M" % count, "clouds": count, "points": total_pts,
+                   "float32_clouds": int((types == 0).sum()), "grids_128_64": int(grid_pick.sum()),
+                   "lanes": args.lanes, "memory_budget_gb": args.budget_gb, "generator_seed": FORM_SEED,
+                   "l2": "inputs larger than L2 (%.1f GB of clouds per step)" % (in_bytes / 1e9)},
+        "e2e": {"value": round(total_pts / b_s / 1e6, 3), "unit": "Mpts/s", "h2d_bytes_per_step": in_bytes,
+                "d2h_bytes_per_step": out_bytes, "ms": round(b_s * 1e3, 2)},
+        "plain_sequential": {"value": round(total_pts / p_s / 1e6, 3), "unit": "Mpts/s", "ms": round(p_s * 1e3, 2)},
+        "speedup_vs_plain": round(p_s / b_s, 3),
+        "per_build_ms": {"p50": round(float(np.percentile([r.runMs for r in res], 50)), 3),
+                         "p99": round(float(np.percentile([r.runMs for r in res], 99)), 3)},
+        "gen_s": round(gen_s, 1), "clocks": clk})
+    print(json.dumps(line))
+    return 0
+
+
+def run_served(args):
+    """A Poisson stream of build requests (sizes log-uniform 100k-30M over a
+    pool of distinct seeded clouds, mixed float32/float64, mixed grids and
+    subsampling options) against a server with a 150 GB device budget."""
+    import concurrent.futures
+    import octree_api
+    import queue
+
+    threads = os.cpu_count() or 1
+    rng = np.random.default_rng(FORM_SEED + 1)
+    pool_n = args.pool
+    sizes = np.exp(rng.uniform(np.log(100_000), np.log(30_000_000), pool_n)).astype(np.int64)
+    types = (rng.random(pool_n) >= 0.8).astype(int)
+    t0 = time.time()
+    pool = [FormCloud(i, i % 3, int(types[i]), int(sizes[i]), FORM_SEED + 1000 + i, threads) for i in range(pool_n)]
+    gen_s = time.time() - t0
+    options = [((512, 128), None), ((128, 64), None), ((512, 128), dict(random=True, intra=True)),
+               ((256, 64), dict(inter=True))]
+    nreq = args.requests
+    req_cloud = rng.integers(0, pool_n, nreq)
+    req_opt = rng.integers(0, len(options), nreq)
+
+    def req_mode(k):
+        o = options[req_opt[k]][1]
+        return o if o is not None else KIND_MODES[pool[req_cloud[k]].kind]
+
+    # shapes of every (cloud, option) pair from plain builds (warm-up)
+    s = octree_api.OctreeSession(0)
+    shape = {}
+    for k in range(nreq):
+        key = (int(req_cloud[k]), int(req_opt[k]))
+        if key not in shape:
+            shape[key] = plain_build(s, pool[key[0]], options[key[1]][0], req_mode(k), None)
+    max_rec = max(p for p, _ in shape.values())
+    max_nodes = max(nn for _, nn in shape.values())
+    slots = args.lanes * 2
+    check_host_memory(slots * max_rec * 18 + sum(c.host.nbytes for c in pool))
+    slot_rec = [pinned_bytes(max_rec * 18) for _ in range(slots)]
+    slot_hier = [np.zeros(max_nodes * 22, np.uint8) for _ in range(slots)]
+    req_pts = np.array([pool[c].n for c in req_cloud], np.int64)
+    total_pts = int(req_pts.sum())
+
+    # plain: every request one at a time (service times, no queueing)
+    plain_ms = []
+    t = time.perf_counter()
+    for k in range(nreq):
+        c = pool[req_cloud[k]]
+        t1 = time.perf_counter()
+        plain_build(s, c, options[req_opt[k]][0], req_mode(k), slot_rec[0], slot_hier[0])
+        plain_ms.append((time.perf_counter() - t1) * 1e3)
+    plain_s = time.perf_counter() - t
+    s.close()
+
+    srv = octree_api.Server(lanes=args.lanes, memory_budget=args.budget_gb << 30)
+
+    def stream(arrivals):
+        """Submits request k at arrivals[k] (seconds from the start) on a free
+        result slot; returns per-request latency (arrival to completion) and
+        the makespan."""
+        free = queue.Queue()
+        for i in range(slots):
+            free.put(i)
+        lat = np.zeros(nreq)
+        done_at = np.zeros(nreq)
+
+        def waiter(k, ticket, slot, t_arr):
+            r = srv.wait(ticket)
+            done_at[k] = time.perf_counter()
+            srv.release(ticket)
+            free.put(slot)
+            if r.status != 0:
+                raise RuntimeError("request %d failed: %s" % (k, r.error.decode()))
+            lat[k] = done_at[k] - t_arr
+
+        with concurrent.futures.ThreadPoolExecutor(max_workers=slots) as ex:
+            futs = []
+            start = time.perf_counter()
+            for k in range(nreq):
+                t_arr = start + arrivals[k]
+                now = time.perf_counter()
+                if t_arr > now:
+                    time.sleep(t_arr - now)
+                slot = free.get()
+                c = pool[req_cloud[k]]
+                job = form_job(c, options[req_opt[k]][0], req_mode(k), slot_rec[slot], slot_hier[slot])
+                futs.append(ex.submit(waiter, k, srv.submit(job), slot, t_arr))
+            for f in futs:
+                f.result()
+        return lat, float(done_at.max() - start)
+
+    # saturation: every request arrives at once
+    stream(np.zeros(nreq))   # warm-up: lanes grow their buffers
+    sat_lat, sat_s = stream(np.zeros(nreq))
+    capacity = total_pts / sat_s
+    # Poisson arrivals at a fraction of the saturation throughput
+    rate = args.load * capacity / (total_pts / nreq)   # requests per second
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, nreq))
+    clocks = ClockSampler(0)
+    clocks.start()
+    lat, span = stream(arrivals)
+    clk = clocks.stop()
+    srv.close()
+    def pct(a_ms, q):
+        return round(float(np.percentile(a_ms, q)), 3)
+
+    lat, sat_lat = lat * 1e3, sat_lat * 1e3
+    line = form_line(args, "Mpts/s served builds, %d Poisson requests" % nreq, total_pts / span / 1e6, "Mpts/s", {
+        "form": "served", "ms_per_step": round(span * 1e3, 2),
+        "config": {"workload": "served_%d_requests_100k_30M" % nreq, "requests": nreq, "points": total_pts,
+                   "distinct_clouds": pool_n, "lanes": args.lanes, "result_slots": slots,
+                   "memory_budget_gb": args.budget_gb, "offered_load": args.load,
+                   "arrival_rate_per_s": round(rate, 2), "generator_seed": FORM_SEED + 1},
+        "latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99)},
+        "saturation": {"value": round(capacity / 1e6, 3), "unit": "Mpts/s", "ms": round(sat_s * 1e3, 2),
+                       "latency_p50_ms": pct(sat_lat, 50), "latency_p99_ms": pct(sat_lat, 99)},
+        "plain_sequential": {"value": round(total_pts / plain_s / 1e6, 3), "unit": "Mpts/s",
+                             "ms": round(plain_s * 1e3, 2), "service_p50_ms": pct(plain_ms, 50),
+                             "service_p99_ms": pct(plain_ms, 99)},
+        "speedup_vs_plain": round(plain_s / sat_s, 3),
+        "e2e": {"value": round(total_pts / span / 1e6, 3), "unit": "Mpts/s",
+                "h2d_bytes_per_step": int(sum(pool[c].n * pool[c].stride for c in req_cloud)),
+                "d2h_bytes_per_step": None},
+        "gen_s": round(gen_s, 1), "clocks": clk})
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -188,11 +492,23 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--points", type=int, default=N_POINTS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--form", default="plain", choices=["plain", "batched", "served"],
+                    help="plain: the 120M-point build; batched / served: many independent builds at once")
+    ap.add_argument("--lanes", type=int, default=4, help="concurrent builds of the batched and served forms")
+    ap.add_argument("--budget-gb", type=int, default=150, help="device memory budget of the batched / served forms")
+    ap.add_argument("--clouds", type=int, default=256, help="clouds of the batched form")
+    ap.add_argument("--requests", type=int, default=2000, help="requests of the served form")
+    ap.add_argument("--pool", type=int, default=24, help="distinct clouds the served requests draw from")
+    ap.add_argument("--load", type=float, default=0.8, help="served offered load, fraction of saturation")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference_arm(args)
+    if args.form == "batched":
+        return run_batched(args)
+    if args.form == "served":
+        return run_served(args)
 
     import octree_api
 

