@@ -318,12 +318,12 @@ struct WeightedSum {
 // of the cluster, and cluster barriers separate the phases.
 template <bool kF32, int kColor, bool kRandom, bool kCluster>
 __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
-    static_assert(!(kCluster && kColor == 3), "weighted averaging runs one block per node");
     namespace cg = cooperative_groups;
     extern __shared__ uint64_t dyn[];
     __shared__ NodeShared ns;
     __shared__ uint32_t warp_sums[32];
     __shared__ uint32_t s_bricks, s_overflow;
+    __shared__ uint32_t s_run_total, s_run_off;   // weighted: this block's run of cells in the CSR scan
     const uint32_t csize = kCluster ? cg::this_cluster().num_blocks() : 1u;
     const uint32_t crank = kCluster ? cg::this_cluster().block_rank() : 0u;
     const uint32_t tid0 = crank * blockDim.x + threadIdx.x;   // this thread's index within the node's workers
@@ -576,27 +576,47 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
             sync_all();
         }
 
-        // ---- weighted: group candidates by cell (CSR)
+        // ---- weighted: group candidates by cell (CSR).  The exclusive scan of
+        // the per-cell counts: each block of a cluster scans a contiguous run
+        // of cells, offset by the totals of the runs before it (read from the
+        // other blocks' shared memory).
         if (weighted) {
+            const uint32_t per = (cells + csize - 1) / csize;
+            const uint32_t c_first = min(cells, crank * per), c_last = min(cells, c_first + per);
             uint32_t running = 0;
-            for (uint32_t base = 0; base < cells; base += blockDim.x) {
+            if constexpr (kCluster) {
+                uint32_t part = 0;
+                for (uint32_t r = c_first + threadIdx.x; r < c_last; r += blockDim.x) part += a.csr_count[off + r];
+                uint32_t total;
+                block_exclusive_scan(part, warp_sums, total);
+                if (threadIdx.x == 0) s_run_total = total;
+                cg::this_cluster().sync();
+                if (threadIdx.x == 0) {
+                    uint32_t o = 0;
+                    for (uint32_t q = 0; q < crank; ++q) o += *cg::this_cluster().map_shared_rank(&s_run_total, q);
+                    s_run_off = o;
+                }
+                __syncthreads();
+                running = s_run_off;
+            }
+            for (uint32_t base = c_first; base < c_last; base += blockDim.x) {
                 uint32_t r = base + threadIdx.x;
-                uint32_t v = r < cells ? a.csr_count[off + r] : 0;
+                uint32_t v = r < c_last ? a.csr_count[off + r] : 0;
                 uint32_t total;
                 uint32_t pre = block_exclusive_scan(v, warp_sums, total);
-                if (r < cells) {
+                if (r < c_last) {
                     a.csr_start[off + r] = running + pre;
                     a.csr_count[off + r] = 0;
                 }
                 running += total;
             }
-            __syncthreads();
+            sync_all();
             for (uint32_t c = 0; c < ns.nchild; ++c) {
                 const uint32_t cnt = ns.count[c];
                 const uint64_t start = ns.start[c];
                 const uint32_t jbase = ns.prefix[c];
                 const uint8_t* src_rec = ((ns.kind >> c) & 1u) ? a.stage_rec : a.leaf_rec;
-                for (uint32_t k = threadIdx.x; k < cnt; k += blockDim.x) {
+                for (uint32_t k = tid0; k < cnt; k += tstride) {
                     const uint32_t j = jbase + k;
                     uint32_t kc = a.key_cache[off + j];
                     uint32_t slot = kc >> 6, bit = kc & 63;
@@ -611,7 +631,7 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
                     dst[4] = (uint32_t)src[8];
                 }
             }
-            __syncthreads();
+            sync_all();
         }
 
         // ---- emit one record per occupied cell (thread per cell, rank order;
@@ -749,10 +769,9 @@ uint32_t cluster_size(uint32_t n_nodes, int num_sms) {
 
 template <bool kF32, int kColor, bool kRandom>
 void launch_one(const SubLevelArgs& a, int num_sms, size_t smem, cudaStream_t stream) {
-    constexpr bool kCanCluster = kColor != 3;
-    const uint32_t cs = kCanCluster ? cluster_size(a.n_nodes, num_sms) : 1u;
+    const uint32_t cs = cluster_size(a.n_nodes, num_sms);
     if (cs > 1) {
-        auto kern = k_subsample<kF32, kColor, kRandom, kCanCluster>;
+        auto kern = k_subsample<kF32, kColor, kRandom, true>;
         allow_dynamic_smem(reinterpret_cast<const void*>(kern), smem);
         cudaLaunchConfig_t cfg = {};
         cudaLaunchAttribute attr[1];
