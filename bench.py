@@ -34,14 +34,36 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "octree-cuda_gb300"))
 
-N_POINTS = 119_701_547
-STRIDE = 27
-CLOUD_TYPE = 1
-SCALE = float(np.float32(0.01))   # the CLI passes the scale through a float (src/argparser.h:12)
-SEED = 20240601
-CFG = dict(chunk_grid=512, merge_threshold=10000, output_factor=2.2, sub_grid=128, inter=True, replacement=True)
-WORKLOAD = "lod_build_120M_f64_terrain_zipf"
-CPU_SAMPLE = 12_000_000   # points of the same cloud timed on the CPU oracle
+# The plain workloads (seeded synthetic clouds of the reference datasets'
+# sizes and types); C is the headline.  Scales are float values widened to
+# double, as the CLI passes them (src/argparser.h:12).
+BASE_CFG = dict(chunk_grid=512, merge_threshold=10000, output_factor=2.2, sub_grid=128, replacement=True)
+WORKLOADS = {
+    "C": dict(name="lod_build_120M_f64_terrain_zipf", n=119_701_547, kind=2, cloud_type=1, stride=27, scale=0.01,
+              seed=20240601, cpu_sample=12_000_000, modes=dict(inter=True)),
+    "A": dict(name="lod_build_5M_f32_heightfield_boxes", n=5_138_448, kind=0, cloud_type=0, stride=15, scale=0.001,
+              seed=20240602, cpu_sample=5_138_448, modes=dict(inter=True)),
+    "B1": dict(name="lod_build_26M_f32_planes_random_intra", n=25_836_417, kind=1, cloud_type=0, stride=15,
+               scale=0.001, seed=20240603, cpu_sample=8_000_000, modes=dict(random=True, intra=True)),
+    "B2": dict(name="lod_build_26M_f32_planes_random_inter_weighted", n=25_836_417, kind=1, cloud_type=0, stride=15,
+               scale=0.001, seed=20240603, cpu_sample=4_000_000, modes=dict(random=True, inter=True, weighting=True)),
+}
+
+
+def metric_name():
+    return "Mpts/s octree build @120M pts" if WORKLOAD == WORKLOADS["C"]["name"] else "Mpts/s octree build @" + WORKLOAD
+
+
+def select_workload(key):
+    """Sets the module's workload constants (N_POINTS, STRIDE, ...)."""
+    global N_POINTS, STRIDE, CLOUD_TYPE, SCALE, SEED, CFG, WORKLOAD, CPU_SAMPLE, KIND
+    w = WORKLOADS[key]
+    N_POINTS, STRIDE, CLOUD_TYPE, KIND = w["n"], w["stride"], w["cloud_type"], w["kind"]
+    SCALE, SEED, WORKLOAD, CPU_SAMPLE = float(np.float32(w["scale"])), w["seed"], w["name"], w["cpu_sample"]
+    CFG = dict(BASE_CFG, **w["modes"])
+
+
+select_workload("C")
 
 
 def peaks():
@@ -133,7 +155,7 @@ def make_cloud(n, threads):
     import octree_api
 
     t = time.time()
-    cloud = octree_api.synthetic_cloud(2, CLOUD_TYPE, n, SEED, STRIDE, threads)
+    cloud = octree_api.synthetic_cloud(KIND, CLOUD_TYPE, n, SEED, STRIDE, threads)
     bb = octree_api.cubic_bbox(cloud, n, STRIDE, CLOUD_TYPE, threads)
     return cloud, bb, time.time() - t
 
@@ -143,7 +165,11 @@ def cpu_oracle_time(cloud, bb, n_sample, threads):
     import oracle
 
     sample = cloud[: n_sample * STRIDE]
-    flags = oracle.F_INTER | oracle.F_REPLACE
+    flags = oracle.F_REPLACE
+    for key, bit in (("intra", oracle.F_INTRA), ("inter", oracle.F_INTER), ("random", oracle.F_RANDOM),
+                     ("weighting", oracle.F_WEIGHT)):
+        if CFG.get(key):
+            flags |= bit
     t = time.perf_counter()
     r = oracle.run(sample, n=n_sample, stride=STRIDE, cloud_type=CLOUD_TYPE, scale=[SCALE] * 3, bb_min=bb[:3],
                    bb_max=bb[3:], chunk_grid=CFG["chunk_grid"], sub_grid=CFG["sub_grid"],
@@ -168,12 +194,14 @@ def run_reference_arm(args):
     t = statistics.median(times)
     v = sample / t / 1e6
     line = {
-        "impl": "reference", "metric": "Mpts/s octree build @120M pts", "value": round(v, 3), "unit": "Mpts/s",
+        "impl": "reference", "metric": metric_name(), "value": round(v, 3), "unit": "Mpts/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t * 1e3, 3),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if CLOUD_TYPE == 1 else "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "points": N_POINTS, "sample_points": sample, **CFG},
         "cpu_baseline": {"value": round(v, 3), "unit": "Mpts/s", "cores": threads, "kind": "port",
-                         "sample": "first %d points of the seeded 119.7M-point cloud, same bbox and settings" % sample},
+                         "sample": "first %d points of the seeded %.1fM-point cloud, same bbox and settings" %
+                                   (sample, N_POINTS / 1e6)},
         "e2e": {"value": round(v, 3), "unit": "Mpts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -191,6 +219,7 @@ def run_reference_arm(args):
 KIND_MODES = {0: dict(inter=True), 1: dict(random=True, inter=True, weighting=True), 2: dict(inter=True)}
 KIND_SCALE = {0: float(np.float32(0.001)), 1: float(np.float32(0.001)), 2: float(np.float32(0.01))}
 FORM_SEED = 20240701
+L2_BYTES = 129 << 20
 
 
 def mode_flags(m):
@@ -490,7 +519,9 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--points", type=int, default=N_POINTS)
+    ap.add_argument("--workload", default="C", choices=sorted(WORKLOADS),
+                    help="C: the headline 119.7M-point float64 build; A, B1, B2: the other plain workloads")
+    ap.add_argument("--points", type=int, default=None, help="point amount (default: the workload's)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--form", default="plain", choices=["plain", "batched", "served"],
                     help="plain: the 120M-point build; batched / served: many independent builds at once")
@@ -502,6 +533,9 @@ def main():
     ap.add_argument("--pool", type=int, default=24, help="distinct clouds the served requests draw from")
     ap.add_argument("--load", type=float, default=0.8, help="served offered load, fraction of saturation")
     args = ap.parse_args()
+    select_workload(args.workload)
+    if args.points is None:
+        args.points = N_POINTS
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
@@ -544,7 +578,18 @@ def main():
     for _ in range(args.warmup):
         s.generate()
 
-    # ---- device-resident build: CUDA events of the builder stream
+    # ---- device-resident build: CUDA events of the builder stream.  A cloud
+    # smaller than twice the L2 is evicted before every timed build by
+    # writing a 512 MB buffer (outside the timed events).
+    cloud_bytes = n * STRIDE
+    flush = None
+    if cloud_bytes < 2 * L2_BYTES:
+        import torch
+
+        flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda:%d" % device)
+        l2_note = "L2 flushed before every timed build (512 MB write; %.0f MB cloud)" % (cloud_bytes / 1e6)
+    else:
+        l2_note = "inputs larger than L2 (%.1f GB cloud)" % (cloud_bytes / 1e9)
     clocks = ClockSampler(device)
     clocks.start()
     barrier()
@@ -552,6 +597,9 @@ def main():
     gen_ms = []
     wall0 = time.perf_counter()
     for _ in range(args.steps):
+        if flush is not None:
+            flush.zero_()
+            torch.cuda.synchronize(device)
         s.generate()
         t = s.timings()
         gen_ms.append(sum(t.values()))
@@ -612,6 +660,8 @@ def main():
     achieved = sb[dom] / (stage_ms[dom] * 1e-3) / 1e9
     traffic = None
     try:
+        if WORKLOAD != WORKLOADS["C"]["name"]:
+            raise KeyError("the DRAM capture covers the headline workload only")
         # DRAM bytes per point of the stage, from one ncu capture of this
         # workload (profiles/dram_traffic_lod_build_120M_f64.md), scaled to n
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
@@ -622,11 +672,11 @@ def main():
         pass
     total_alg = sum(sb.values())
     line = {
-        "metric": "Mpts/s octree build @120M pts", "value": round(value, 3), "unit": "Mpts/s", "n_gpus": ws,
+        "metric": metric_name(), "value": round(value, 3), "unit": "Mpts/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if CLOUD_TYPE == 1 else "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "points": n, "record_bytes": STRIDE, "scale": SCALE, **CFG,
-                   "l2": "inputs larger than L2 (3.2 GB cloud)", "generator_seed": SEED},
+                   "l2": l2_note, "generator_seed": SEED},
         "gpu_launches": int(st.get("kernel_launches", 0)) * args.steps,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": peak_kind,
