@@ -327,17 +327,23 @@ def run_batched(args):
     modes = [KIND_MODES[c.kind] for c in clouds]
     total_pts = int(sizes.sum())
 
-    # output sizes from one plain pass (warm-up), then exact pinned outputs
+    # output sizes from one plain pass (warm-up), then exact pinned outputs;
+    # --no-plain: results stay on the device (no plain builds at all)
     s = octree_api.OctreeSession(0)
-    shapes = []
-    for c, g, m in zip(clouds, grids, modes):
-        shapes.append(plain_build(s, c, g, m, None))
-    need = sum(max(p, 1) * 18 for p, _ in shapes)
-    check_host_memory(need + sum(c.host.nbytes for c in clouds))
-    recs = [pinned_bytes(max(p, 1) * 18) for p, _ in shapes]
-    hiers = [np.zeros(nn * 22, np.uint8) for _, nn in shapes]
-    out_bytes = sum(p * 18 + nn * 22 for p, nn in shapes)
     in_bytes = sum(c.n * c.stride for c in clouds)
+    if args.no_plain:
+        recs = [None] * count
+        hiers = [None] * count
+        out_bytes = 0
+    else:
+        shapes = []
+        for c, g, m in zip(clouds, grids, modes):
+            shapes.append(plain_build(s, c, g, m, None))
+        need = sum(max(p, 1) * 18 for p, _ in shapes)
+        check_host_memory(need + sum(c.host.nbytes for c in clouds))
+        recs = [pinned_bytes(max(p, 1) * 18) for p, _ in shapes]
+        hiers = [np.zeros(nn * 22, np.uint8) for _, nn in shapes]
+        out_bytes = sum(p * 18 + nn * 22 for p, nn in shapes)
 
     def plain_pass():
         t = time.perf_counter()
@@ -356,9 +362,10 @@ def run_batched(args):
             raise RuntimeError("batched build failed: %s" % bad[0])
         return dt, res
 
-    for _ in range(max(1, args.warmup - 1)):
-        plain_pass()
-    plain_s = [plain_pass() for _ in range(args.steps)]
+    if not args.no_plain:
+        for _ in range(max(1, args.warmup - 1)):
+            plain_pass()
+    plain_s = [plain_pass() for _ in range(args.steps)] if not args.no_plain else [float("nan")]
     for _ in range(args.warmup):
         batch_pass()
     clocks = ClockSampler(0)
@@ -377,8 +384,9 @@ def run_batched(args):
                    "l2": "inputs larger than L2 (%.1f GB of clouds per step)" % (in_bytes / 1e9)},
         "e2e": {"value": round(total_pts / b_s / 1e6, 3), "unit": "Mpts/s", "h2d_bytes_per_step": in_bytes,
                 "d2h_bytes_per_step": out_bytes, "ms": round(b_s * 1e3, 2)},
-        "plain_sequential": {"value": round(total_pts / p_s / 1e6, 3), "unit": "Mpts/s", "ms": round(p_s * 1e3, 2)},
-        "speedup_vs_plain": round(p_s / b_s, 3),
+        "plain_sequential": None if args.no_plain else
+        {"value": round(total_pts / p_s / 1e6, 3), "unit": "Mpts/s", "ms": round(p_s * 1e3, 2)},
+        "speedup_vs_plain": None if args.no_plain else round(p_s / b_s, 3),
         "per_build_ms": {"p50": round(float(np.percentile([r.runMs for r in res], 50)), 3),
                          "p99": round(float(np.percentile([r.runMs for r in res], 99)), 3)},
         "gen_s": round(gen_s, 1), "clocks": clk})
@@ -532,6 +540,8 @@ def main():
     ap.add_argument("--requests", type=int, default=2000, help="requests of the served form")
     ap.add_argument("--pool", type=int, default=24, help="distinct clouds the served requests draw from")
     ap.add_argument("--load", type=float, default=0.8, help="served offered load, fraction of saturation")
+    ap.add_argument("--no-plain", action="store_true",
+                    help="batched form only: no plain comparison and no host outputs (for profiling)")
     args = ap.parse_args()
     select_workload(args.workload)
     if args.points is None:

@@ -75,3 +75,47 @@ def test_memory_estimate_reference_formula():
     assert g2 > gb300 and r2 > ref
     with pytest.raises(octree_api.OctreeError):
         octree_api.estimate_memory(n, stride, 1, 500, 10000, 2.2, 128, 0)   # grid not a power of two
+
+
+def test_server_and_batch_argument_errors_without_gpu():
+    """The batched and served entry points check their arguments before any
+    CUDA call and report through the return code."""
+    L = octree_api.load_library()
+    assert L.ocpi_server_create(None, 0, 4, 1 << 30) == -1
+    assert b"null server pointer" in L.ocpi_last_error()
+    h = ctypes.c_void_p()
+    assert L.ocpi_server_create(ctypes.byref(h), 0, 0, 1 << 30) == -1
+    assert b"lanes" in L.ocpi_last_error()
+    assert L.ocpi_batch_build(0, 4, 1 << 30, None, 0, None) == -1
+    assert b"null argument" in L.ocpi_last_error()
+    t = ctypes.c_uint64()
+    assert L.ocpi_server_submit(None, ctypes.byref(octree_api.OcpiJob()), ctypes.byref(t)) == -1
+    assert L.ocpi_server_wait(None, 1, None) == -1
+    assert L.ocpi_server_release(None, 1) == -1
+
+
+def test_job_structs_match_the_header(tmp_path):
+    """ctypes layouts of OcpiJob / OcpiJobResult against the C compiler's."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    fields = {"OcpiJob": [f for f, _ in octree_api.OcpiJob._fields_],
+              "OcpiJobResult": [f for f, _ in octree_api.OcpiJobResult._fields_]}
+    src = ['#include <stdio.h>', '#include <stddef.h>', '#include "octreeApi.h"', 'int main(void) {']
+    for st, fs in fields.items():
+        src.append('printf("%%zu\\n", sizeof(%s));' % st)
+        src += ['printf("%%zu\\n", offsetof(%s, %s));' % (st, f) for f in fs]
+    src.append("return 0; }")
+    c = tmp_path / "layout.c"
+    c.write_text("\n".join(src))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(c), "-o", str(exe)], check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
+    want = []
+    for st in (octree_api.OcpiJob, octree_api.OcpiJobResult):
+        want.append(ctypes.sizeof(st))
+        want += [getattr(st, f).offset for f, _ in st._fields_]
+    assert got == want
