@@ -622,6 +622,10 @@ void Builder::build_tree_host() {
         check_cuda(cudaStreamSynchronize(stream_), "tree");
         throw Error("counting: node capacity exceeded");
     }
+    if (e) {   // counting failed (a point below the box, a bulk copy timed out): stop before the host tree
+        check_cuda(cudaStreamSynchronize(stream_), "tree");
+        throw_device_errors(e, "counting");
+    }
     if (n > node_cap_) throw Error("counting: node count out of range");
     // pinned layout: key, count, child_first (u32), info (u16), level (u8),
     // occupied cells per level (u32)

@@ -113,17 +113,25 @@ public:
         for (auto& t : workers_) t.join();
     }
 
+    // Throws what submit() refuses: an invalid configuration, no cloud, or a
+    // memory bound above the budget.
+    void check(const OcpiJob& spec) const {
+        const BuildConfig cfg = config_of(spec);
+        cfg.validate();
+        if (!spec.cloud) throw Error("job without a point cloud");
+        const uint64_t bound = device_bytes(memory_terms(cfg, sms_));
+        if (bound > budget_)
+            throw Error("job needs up to " + std::to_string(bound) + " device bytes, above the executor budget of " +
+                        std::to_string(budget_));
+    }
+
     uint64_t submit(const OcpiJob& spec) {
+        check(spec);
         auto job = std::make_shared<Job>();
         job->spec = spec;
         job->cfg = config_of(spec);
-        job->cfg.validate();
-        if (!spec.cloud) throw Error("job without a point cloud");
         job->terms = memory_terms(job->cfg, sms_);
         job->bound = device_bytes(job->terms);
-        if (job->bound > budget_)
-            throw Error("job needs up to " + std::to_string(job->bound) + " device bytes, above the executor budget of " +
-                        std::to_string(budget_));
         std::lock_guard<std::mutex> g(mu_);
         job->ticket = ++next_ticket_;
         job->submitted = Clock::now();
@@ -377,6 +385,15 @@ int ocpi_batch_build(int device, uint32_t lanes, uint64_t memoryBudget, const Oc
         if (!jobs || !results) throw oc::Error("null argument");
         if (lanes < 1 || lanes > 64) throw oc::Error("lanes must be in [1, 64]");
         oc::Executor& ex = oc::batch_executor(device, lanes, memoryBudget);
+        // every job is checked before any starts: a refused job leaves no
+        // other job of the batch running after the call returns
+        for (uint32_t i = 0; i < count; ++i) {
+            try {
+                ex.check(jobs[i]);
+            } catch (const std::exception& e) {
+                throw oc::Error("job " + std::to_string(i) + " of the batch: " + e.what());
+            }
+        }
         std::vector<uint64_t> tickets(count);
         for (uint32_t i = 0; i < count; ++i) tickets[i] = ex.submit(jobs[i]);
         bool ok = true;

@@ -87,3 +87,33 @@ def test_server_admission_under_a_small_budget():
     with pytest.raises(octree_api.OctreeError, match="budget"):
         srv.submit(job_for(big, (512, 128), 0, None, None, None))
     srv.close()
+
+
+def test_failed_job_leaves_the_batch_intact():
+    """One job whose box leaves points below it fails with the device's
+    error; the other jobs of the batch still equal their builds alone."""
+    cases = mixed_cases(6)
+    want = [alone(c, g, m) for c, g, m in cases]
+    bufs = [buffers(w) for w in want]
+    jobs = [job_for(c, g, m, *b) for (c, g, m), b in zip(cases, bufs)]
+    bad, g, m = cases[2]
+    shift = (bad.bb_max[0] - bad.bb_min[0]) / 4
+    jobs[2] = octree_api.make_job(bad.cloud, n=bad.n, stride=bad.stride, cloud_type=bad.cloud_type, scale=bad.scale,
+                                  bb_min=[v + shift for v in bad.bb_min], bb_max=[v + shift for v in bad.bb_max],
+                                  chunk_grid=g[0], sub_grid=g[1], merge_threshold=2000, flags=FLAGS[m], seed=99)
+    results = octree_api.batch_build(jobs, lanes=3)
+    assert results[2].status == -1 and b"below the bounding box" in results[2].error
+    for i, (w, r, b) in enumerate(zip(want, results, bufs)):
+        if i != 2:
+            check_same(w, r, *b)
+
+
+def test_batch_refuses_an_invalid_job_before_starting_any():
+    cases = mixed_cases(3)
+    want = [alone(c, g, m) for c, g, m in cases]
+    bufs = [buffers(w) for w in want]
+    jobs = [job_for(c, g, m, *b) for (c, g, m), b in zip(cases, bufs)]
+    jobs[1].chunkingGrid = 96   # not a power of two
+    with pytest.raises(octree_api.OctreeError, match="job 1 of the batch"):
+        octree_api.batch_build(jobs, lanes=2)
+    assert all(not np.any(b[0]) for b in bufs), "a job ran although the batch was refused"
