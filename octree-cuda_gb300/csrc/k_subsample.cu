@@ -155,10 +155,6 @@ __device__ __forceinline__ float quant_units(int32_t q, const QAxis& a) {
     return __fmaf_rn(__fadd_rn((float)(q - a.qn), 0.5f), a.B, a.base);
 }
 
-__device__ __forceinline__ int32_t rec_coord(const uint16_t* r, int i) {
-    return (int32_t)((uint32_t)r[2 * i] | ((uint32_t)r[2 * i + 1] << 16));
-}
-
 struct NodeShared {
     uint64_t start[8];
     uint32_t count[8];
@@ -284,12 +280,6 @@ __device__ __forceinline__ uint64_t inter_sum(const BrickMap& bm, uint32_t slot,
     }
     return e;
 }
-
-struct InterSum {
-    const uint64_t* acc;
-    uint64_t e;
-    __device__ __forceinline__ void operator()(uint32_t n, int, int, int) { e += acc[n]; }
-};
 
 struct WeightedSum {
     const uint32_t* start;
