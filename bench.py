@@ -292,13 +292,13 @@ def ctypes_u64():
     return ctypes.c_uint64()
 
 
-def form_job(c, grids, mode, rec, hier):
+def form_job(c, grids, mode, rec, hier, cloud_id=0):
     import octree_api
 
     return octree_api.make_job(c.host, n=c.n, stride=c.stride, cloud_type=c.cloud_type, scale=[c.scale] * 3,
                                bb_min=c.bb[:3], bb_max=c.bb[3:], chunk_grid=grids[0], merge_threshold=10000,
                                output_factor=2.2, sub_grid=grids[1], flags=mode_flags(mode), seed=c.seed,
-                               records=rec, hierarchy=hier)
+                               records=rec, hierarchy=hier, cloud_id=cloud_id)
 
 
 def form_line(args, metric, value, unit, extra):
@@ -458,10 +458,12 @@ def run_served(args):
             free.put(i)
         lat = np.zeros(nreq)
         done_at = np.zeros(nreq)
+        reused = np.zeros(nreq, np.int64)
 
         def waiter(k, ticket, slot, t_arr):
             r = srv.wait(ticket)
             done_at[k] = time.perf_counter()
+            reused[k] = r.reused
             srv.release(ticket)
             free.put(slot)
             if r.status != 0:
@@ -478,22 +480,23 @@ def run_served(args):
                     time.sleep(t_arr - now)
                 slot = free.get()
                 c = pool[req_cloud[k]]
-                job = form_job(c, options[req_opt[k]][0], req_mode(k), slot_rec[slot], slot_hier[slot])
+                job = form_job(c, options[req_opt[k]][0], req_mode(k), slot_rec[slot], slot_hier[slot],
+                               cloud_id=0 if args.no_resident else int(req_cloud[k]) + 1)
                 futs.append(ex.submit(waiter, k, srv.submit(job), slot, t_arr))
             for f in futs:
                 f.result()
-        return lat, float(done_at.max() - start)
+        return lat, float(done_at.max() - start), int(reused.sum())
 
     # saturation: every request arrives at once
     stream(np.zeros(nreq))   # warm-up: lanes grow their buffers
-    sat_lat, sat_s = stream(np.zeros(nreq))
+    sat_lat, sat_s, sat_reused = stream(np.zeros(nreq))
     capacity = total_pts / sat_s
     # Poisson arrivals at a fraction of the saturation throughput
     rate = args.load * capacity / (total_pts / nreq)   # requests per second
     arrivals = np.cumsum(rng.exponential(1.0 / rate, nreq))
     clocks = ClockSampler(0)
     clocks.start()
-    lat, span = stream(arrivals)
+    lat, span, reused = stream(arrivals)
     clk = clocks.stop()
     srv.close()
     def pct(a_ms, q):
@@ -505,8 +508,10 @@ def run_served(args):
         "config": {"workload": "served_%d_requests_100k_30M" % nreq, "requests": nreq, "points": total_pts,
                    "distinct_clouds": pool_n, "lanes": args.lanes, "result_slots": slots,
                    "memory_budget_gb": args.budget_gb, "offered_load": args.load,
+                   "cloud_ids": not args.no_resident,
                    "arrival_rate_per_s": round(rate, 2), "generator_seed": FORM_SEED + 1},
         "latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99)},
+        "resident_reuse": {"poisson": reused, "saturation": sat_reused, "requests": nreq},
         "saturation": {"value": round(capacity / 1e6, 3), "unit": "Mpts/s", "ms": round(sat_s * 1e3, 2),
                        "latency_p50_ms": pct(sat_lat, 50), "latency_p99_ms": pct(sat_lat, 99)},
         "plain_sequential": {"value": round(total_pts / plain_s / 1e6, 3), "unit": "Mpts/s",
@@ -540,6 +545,8 @@ def main():
     ap.add_argument("--requests", type=int, default=2000, help="requests of the served form")
     ap.add_argument("--pool", type=int, default=24, help="distinct clouds the served requests draw from")
     ap.add_argument("--load", type=float, default=0.8, help="served offered load, fraction of saturation")
+    ap.add_argument("--no-resident", action="store_true",
+                    help="served form: requests carry no cloud id, so no lane reuses a resident cloud")
     ap.add_argument("--no-plain", action="store_true",
                     help="batched form only: no plain comparison and no host outputs (for profiling)")
     args = ap.parse_args()

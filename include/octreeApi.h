@@ -182,12 +182,15 @@ typedef struct OcpiJob {
     uint64_t outCapacity;      /* records */
     uint8_t* outHierarchy;     /* optional host array for hierarchy.bin */
     uint64_t outHierarchyCapacity;   /* bytes */
+    uint64_t cloudId;          /* 0, or an id naming this cloud's contents: a lane that built the same id with the
+                                  same chunking settings reruns only subsampling on its resident device state */
 } OcpiJob;
 
 typedef struct OcpiJobResult {
     int32_t status;            /* 0 = built, -1 = failed (error holds the message) */
     uint32_t lane;
     uint32_t nodeCount;        /* hierarchy.bin entries */
+    uint32_t reused;           /* 1: subsampled the lane's resident cloud state (no upload, counting or distribution) */
     uint64_t pointsTotal;      /* octree.bin records */
     double queuedMs;           /* submission to start */
     double runMs;              /* start to completion (upload, build, read-back) */

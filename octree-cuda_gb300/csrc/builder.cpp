@@ -197,6 +197,9 @@ Builder::Builder(const BuildConfig& cfg, const uint8_t* host_cloud, int device) 
 // grows, so a builder that has served larger builds allocates nothing.
 void Builder::reconfigure(const BuildConfig& cfg, const uint8_t* host_cloud, bool wait_upload) {
     cfg.validate();
+    tree_valid_ = false;
+    reuse_tree_ = false;
+    bbox_from_device_ = false;
     if (copy_stream_) check_cuda(cudaStreamSynchronize(copy_stream_), "output copies");
     cfg_ = cfg;
     host_rec_ = nullptr;
@@ -288,6 +291,8 @@ void Builder::fill_cell_tables() {
 // calculateRealBB + calculateCubicBB (src/boundingbox.h:11-52) over the
 // uploaded cloud; the cubic box becomes the build's bounding box.
 void Builder::compute_bbox(double real[6], double cubic[6]) {
+    tree_valid_ = false;
+    reuse_tree_ = false;
     bbox_keys_.ensure(6 * 8);
     launches_ = 0;
     launch_bbox(cloud_.as<uint8_t>(), cfg_.n, cfg_.stride, cfg_.cloud_type == 0, bbox_keys_.as<long long>(), num_sms_,
@@ -319,6 +324,37 @@ void Builder::compute_bbox(double real[6], double cubic[6]) {
     params_writable();
     fill_cell_tables();
     record_params();
+    bbox_from_device_ = true;
+}
+
+bool Builder::reuse(const BuildConfig& c) {
+    if (!tree_valid_) return false;
+    c.validate();
+    const BuildConfig& r = cfg_;
+    bool same = c.n == r.n && c.stride == r.stride && c.cloud_type == r.cloud_type && c.chunk_grid == r.chunk_grid &&
+                c.threshold == r.threshold && c.debug == r.debug;
+    for (int a = 0; a < 3; ++a) same = same && c.scale[a] == r.scale[a];
+    if (c.has_bbox()) {
+        for (int a = 0; a < 3; ++a) same = same && c.bb_min[a] == r.bb_min[a] && c.bb_max[a] == r.bb_max[a];
+    } else {
+        same = same && bbox_from_device_;
+    }
+    if (!same) return false;
+    if (copy_stream_) check_cuda(cudaStreamSynchronize(copy_stream_), "output copies");
+    cfg_.output_factor = c.output_factor;
+    cfg_.sub_grid = c.sub_grid;
+    cfg_.intra = c.intra;
+    cfg_.inter = c.inter;
+    cfg_.replacement = c.replacement;
+    cfg_.random = c.random;
+    cfg_.weighting = c.weighting;
+    cfg_.seed = c.seed;
+    host_rec_ = nullptr;
+    host_lut_ = nullptr;
+    host_cap_ = 0;
+    host_filled_ = false;
+    reuse_tree_ = true;
+    return true;
 }
 
 Builder::~Builder() {
@@ -497,6 +533,8 @@ void Builder::set_output_host(uint8_t* records, uint32_t* lut, uint64_t capacity
 
 void Builder::upload(const uint8_t* host_cloud, bool wait) {
     if (!host_cloud) throw Error("no point cloud set");
+    tree_valid_ = false;
+    reuse_tree_ = false;
     if (!wait) {
         check_cuda(cudaMemcpyAsync(cloud_.p, host_cloud, (size_t)cfg_.n * cfg_.stride, cudaMemcpyHostToDevice, stream_),
                    "cloud upload");
@@ -530,6 +568,24 @@ void throw_device_errors(uint32_t e, const char* stage) {
 void Builder::generate() {
     host_filled_ = false;
     sub_err_valid_ = false;
+    if (reuse_tree_) {
+        // the cloud, pyramid, tree and leaf records of this configuration are
+        // on the device: subsample them with the new settings
+        reuse_tree_ = false;
+        tree_valid_ = false;
+        if (host_rec_ && host_cap_ < cfg_.n) throw Error("output host buffer holds fewer records than the cloud");
+        stage_begin();
+        launches_ = 0;
+        subsample();
+        check_cuda(cudaGetLastError(), "launch");
+        if (sub_err_valid_) throw_device_errors(sub_err_, "generate");
+        else check_device_errors("generate");
+        collect_timings();
+        compute_stats();
+        tree_valid_ = true;
+        return;
+    }
+    tree_valid_ = false;
     if (!cfg_.has_bbox()) throw Error("no bounding box: call ocpi_set_cloud_bb before ocpi_init_octree or ocpi_compute_cloud_bb after it");
     if (host_rec_ && host_cap_ < cfg_.n) throw Error("output host buffer holds fewer records than the cloud");
     const double cubic = cfg_.bb_max[0] - cfg_.bb_min[0];
@@ -607,6 +663,7 @@ void Builder::generate() {
     else check_device_errors("generate");
     collect_timings();
     compute_stats();
+    tree_valid_ = true;
 }
 
 // Host copy of the node table (NodeHost), read on the side stream once tree

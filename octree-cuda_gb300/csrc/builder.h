@@ -138,6 +138,14 @@ public:
     void upload(const uint8_t* host_cloud, bool wait = true);
     // A new configuration and cloud; buffers only grow (see size_for_config).
     void reconfigure(const BuildConfig& cfg, const uint8_t* host_cloud, bool wait_upload = true);
+    // Resident state: after a successful generate(), the uploaded cloud, the
+    // count pyramid, the node tree and the leaf records stay on the device.
+    // If `cfg` differs from the last build only in its subsampling settings
+    // (grid, modes, seed, output factor), reuse() adopts them and the next
+    // generate() runs subsampling alone; otherwise it returns false and
+    // changes nothing.  A job whose box is unset matches a state whose box
+    // was computed on the device.
+    bool reuse(const BuildConfig& cfg);
     void generate();
     // Real and cubic bounding boxes {minX, minY, minZ, maxX, maxY, maxZ} of
     // the uploaded cloud; the cubic box becomes the build's bounding box.
@@ -159,6 +167,7 @@ public:
     // copied while subsampling runs.
     void set_output_host(uint8_t* records, uint32_t* lut, uint64_t capacity);
     bool records_filled(const void* records) const { return host_filled_ && records == host_rec_; }
+    bool reused() const { return reuse_tree_; }
     bool lut_filled(const void* lut) const { return host_filled_ && host_lut_ && lut == host_lut_; }
     const BuildConfig& config() const { return cfg_; }
     // Device memory held by this session: named allocations in bytes.
@@ -215,6 +224,9 @@ private:
     uint32_t nonzero_sum_ = 0;                      // occupied cells over all levels
     uint32_t sub_err_ = 0;                          // device error word read after subsampling
     bool sub_err_valid_ = false;
+    bool tree_valid_ = false;        // the device holds the tree and leaf records of cfg_ (last generate succeeded)
+    bool bbox_from_device_ = false;  // cfg_'s box came from compute_bbox
+    bool reuse_tree_ = false;        // the next generate() subsamples the resident tree
     uint64_t sub_stage_cap_ = 0, sub_scratch_cap_ = 0, sub_rec_cap_ = 0;   // capacities that fit the last build
     uint32_t g_cap_ = 0, g_shift_ = 0;
     uint32_t launches_ = 0;

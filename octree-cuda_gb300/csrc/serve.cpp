@@ -17,6 +17,13 @@
 // bound exceeds the budget alone fails at submission.  An idle lane whose
 // memory keeps a waiting job out frees its builder.
 //
+// Resident clouds: a job may name its cloud (cloudId != 0; equal ids promise
+// equal cloud contents).  A lane remembers the id of the cloud its builder
+// last built; a job with that id and the same chunking settings reruns only
+// subsampling on the resident pyramid, tree and leaf records (Builder::reuse).
+// Among the first waiting jobs, a free lane takes one naming its resident
+// cloud before the oldest.
+//
 // Results do not depend on the mix: each build owns its state, and every
 // kernel is deterministic up to the order of records inside a node.
 #include <algorithm>
@@ -60,6 +67,17 @@ struct Job {
     std::vector<uint8_t> hierarchy;
 };
 
+// The chunking settings of b match those of the resident state built for a
+// (a job without a box may match a state whose box came from the device).
+bool same_chunking(const BuildConfig& a, const BuildConfig& b) {
+    bool same = a.n == b.n && a.stride == b.stride && a.cloud_type == b.cloud_type && a.chunk_grid == b.chunk_grid &&
+                a.threshold == b.threshold;
+    for (int k = 0; k < 3; ++k) same = same && a.scale[k] == b.scale[k];
+    if (a.has_bbox() && b.has_bbox())
+        for (int k = 0; k < 3; ++k) same = same && a.bb_min[k] == b.bb_min[k] && a.bb_max[k] == b.bb_max[k];
+    return same;
+}
+
 BuildConfig config_of(const OcpiJob& j) {
     BuildConfig c;
     c.n = j.pointAmount;
@@ -91,6 +109,8 @@ public:
         check_cuda(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, device), "device attribute");
         reserved_.assign(lanes, 0);
         env_.assign(lanes, MemoryTerms{});
+        resident_.assign(lanes, 0);
+        resident_cfg_.assign(lanes, BuildConfig{});
         busy_.assign(lanes, false);
         releasing_.assign(lanes, false);
         for (uint32_t l = 0; l < lanes; ++l) workers_.emplace_back([this, l] { run_lane(l); });
@@ -169,11 +189,27 @@ public:
     }
 
 private:
-    // The oldest waiting job that fits the budget on lane l (mutex held).
+    // The next job for lane l (mutex held): among the first 2 x lanes waiting
+    // jobs, the oldest that names the lane's resident cloud; else the oldest
+    // waiting job that fits the budget.
     std::shared_ptr<Job> take(uint32_t l) {
         uint64_t others = 0;
         for (size_t k = 0; k < reserved_.size(); ++k)
             if (k != l) others += reserved_[k];
+        if (resident_[l]) {
+            size_t seen = 0;
+            for (auto it = queue_.begin(); it != queue_.end() && seen < 2 * reserved_.size(); ++it, ++seen) {
+                if ((*it)->spec.cloudId != resident_[l] || !same_chunking(resident_cfg_[l], (*it)->cfg)) continue;
+                const MemoryTerms env = envelope(env_[l], (*it)->terms);
+                const uint64_t mine = device_bytes(env);
+                if (others + mine > budget_) continue;
+                auto job = *it;
+                queue_.erase(it);
+                env_[l] = env;
+                reserved_[l] = mine;
+                return job;
+            }
+        }
         for (auto it = queue_.begin(); it != queue_.end(); ++it) {
             const MemoryTerms env = envelope(env_[l], (*it)->terms);
             const uint64_t mine = device_bytes(env);
@@ -235,6 +271,7 @@ private:
                     std::lock_guard<std::mutex> g(mu_);
                     reserved_[l] = 0;
                     env_[l] = MemoryTerms{};
+                    resident_[l] = 0;
                     releasing_[l] = false;
                 }
                 cv_work_.notify_all();
@@ -246,12 +283,22 @@ private:
                 const OcpiJob& s = job->spec;
                 BuildConfig cfg = job->cfg;
                 const bool device_bb = !cfg.has_bbox();
-                if (!builder) builder = std::make_unique<Builder>(cfg, s.cloud, device_);
-                else builder->reconfigure(cfg, s.cloud, false);   // the upload overlaps the set-up
-                if (device_bb) {
-                    double real[6], cubic[6];
-                    builder->compute_bbox(real, cubic);
+                uint64_t had;
+                {
+                    std::lock_guard<std::mutex> g(mu_);
+                    had = resident_[l];
+                    resident_[l] = 0;   // until this job succeeds
                 }
+                const bool reuse = builder && s.cloudId && s.cloudId == had && builder->reuse(cfg);
+                if (!reuse) {
+                    if (!builder) builder = std::make_unique<Builder>(cfg, s.cloud, device_);
+                    else builder->reconfigure(cfg, s.cloud, false);   // the upload overlaps the set-up
+                    if (device_bb) {
+                        double real[6], cubic[6];
+                        builder->compute_bbox(real, cubic);
+                    }
+                }
+                r.reused = reuse ? 1u : 0u;
                 if (s.outRecords) builder->set_output_host(s.outRecords, s.outLut, s.outCapacity);
                 builder->generate();
                 hier = builder->hierarchy();
@@ -262,6 +309,11 @@ private:
                     std::memcpy(s.outHierarchy, hier.data(), hier.size());
                 }
                 const Stats& st = builder->stats();
+                {
+                    std::lock_guard<std::mutex> g(mu_);
+                    resident_[l] = s.cloudId;
+                    resident_cfg_[l] = job->cfg;
+                }
                 r.status = 0;
                 r.nodeCount = st.tree_nodes;
                 r.pointsTotal = st.points_total;
@@ -286,6 +338,7 @@ private:
                 if (!builder) {
                     reserved_[l] = 0;
                     env_[l] = MemoryTerms{};
+                    resident_[l] = 0;
                 }
             }
             cv_done_.notify_all();
@@ -302,6 +355,8 @@ private:
     std::map<uint64_t, std::shared_ptr<Job>> jobs_;
     std::vector<uint64_t> reserved_;   // device bytes held or claimed per lane
     std::vector<MemoryTerms> env_;     // envelope of the jobs each lane's builder has run
+    std::vector<uint64_t> resident_;   // cloud id whose tree each lane's builder holds (0: none)
+    std::vector<BuildConfig> resident_cfg_;   // the configuration that tree was built with
     std::vector<bool> busy_, releasing_;
     std::vector<std::thread> workers_;
     uint64_t next_ticket_ = 0;

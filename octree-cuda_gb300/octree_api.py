@@ -72,13 +72,14 @@ class OcpiJob(ctypes.Structure):
         ("outputFactor", ctypes.c_float), ("subsamplingGrid", ctypes.c_uint32), ("modeFlags", ctypes.c_uint32),
         ("seed", ctypes.c_uint64), ("outRecords", ctypes.c_void_p), ("outLut", ctypes.c_void_p),
         ("outCapacity", ctypes.c_uint64), ("outHierarchy", ctypes.c_void_p), ("outHierarchyCapacity", ctypes.c_uint64),
+        ("cloudId", ctypes.c_uint64),
     ]
 
 
 class OcpiJobResult(ctypes.Structure):
     _fields_ = [
         ("status", ctypes.c_int32), ("lane", ctypes.c_uint32), ("nodeCount", ctypes.c_uint32),
-        ("pointsTotal", ctypes.c_uint64), ("queuedMs", ctypes.c_double), ("runMs", ctypes.c_double),
+        ("reused", ctypes.c_uint32), ("pointsTotal", ctypes.c_uint64), ("queuedMs", ctypes.c_double), ("runMs", ctypes.c_double),
         ("totalMs", ctypes.c_double), ("deviceMs", ctypes.c_double), ("error", ctypes.c_char * 128),
     ]
 
@@ -349,7 +350,8 @@ def build_octree(cloud, *, n, stride, cloud_type, scale, bb_min, bb_max, device=
 
 
 def make_job(cloud, *, n, stride, cloud_type, scale, bb_min=None, bb_max=None, chunk_grid=512, merge_threshold=10000,
-             output_factor=2.2, sub_grid=128, flags=SUB_INTER, seed=0x5EED, records=None, lut=None, hierarchy=None):
+             output_factor=2.2, sub_grid=128, flags=SUB_INTER, seed=0x5EED, records=None, lut=None, hierarchy=None,
+             cloud_id=0):
     """OcpiJob for Server.submit / batch_build.  bb_min None: the box is
     computed on the device.  records / lut / hierarchy: optional host arrays
     the build fills (keep them, and the cloud, alive until it completes)."""
@@ -361,7 +363,7 @@ def make_job(cloud, *, n, stride, cloud_type, scale, bb_min=None, bb_max=None, c
         j.bbMin[:] = [float(v) for v in bb_min]
         j.bbMax[:] = [float(v) for v in bb_max]
     j.chunkingGrid, j.mergingThreshold, j.outputFactor, j.subsamplingGrid = chunk_grid, merge_threshold, output_factor, sub_grid
-    j.modeFlags, j.seed = flags, seed
+    j.modeFlags, j.seed, j.cloudId = flags, seed, cloud_id
     if records is not None:
         j.outRecords, j.outCapacity = records.ctypes.data, len(records) // 18
         j.outLut = lut.ctypes.data if lut is not None else None

@@ -33,11 +33,11 @@ def alone(case, grids, m):
     return h, r, l
 
 
-def job_for(case, grids, m, rec, lut, hier, device_bbox=False):
+def job_for(case, grids, m, rec, lut, hier, device_bbox=False, cloud_id=0):
     kw = {} if device_bbox else dict(bb_min=case.bb_min, bb_max=case.bb_max)
     return octree_api.make_job(case.cloud, n=case.n, stride=case.stride, cloud_type=case.cloud_type, scale=case.scale,
                                chunk_grid=grids[0], sub_grid=grids[1], merge_threshold=2000, flags=FLAGS[m], seed=99,
-                               records=rec, lut=lut, hierarchy=hier, **kw)
+                               records=rec, lut=lut, hierarchy=hier, cloud_id=cloud_id, **kw)
 
 
 def check_same(want, res, rec, lut, hier):
@@ -117,3 +117,34 @@ def test_batch_refuses_an_invalid_job_before_starting_any():
     with pytest.raises(octree_api.OctreeError, match="job 1 of the batch"):
         octree_api.batch_build(jobs, lanes=2)
     assert all(not np.any(b[0]) for b in bufs), "a job ran although the batch was refused"
+
+
+def test_server_reuses_resident_cloud_state():
+    """Jobs naming the same cloud (cloudId) and chunking settings rerun only
+    subsampling on the lane's resident state; every result still equals the
+    build run alone, and state is not reused across clouds, chunking grids or
+    an explicit / device-computed bounding box."""
+    a = make_case(0, 0, 300_000, seed=41)
+    b = make_case(1, 1, 200_000, seed=42)
+    steps = [   # case, grids, mode, cloud id, device box, expected reuse
+        (a, (128, 64), 0, 1, False, 0),
+        (a, (128, 64), 1, 1, False, 1),
+        (a, (128, 64), 2, 1, False, 1),
+        (a, (64, 32), 0, 1, False, 0),
+        (a, (64, 16), 3, 1, False, 1),
+        (b, (128, 64), 0, 2, False, 0),
+        (a, (128, 64), 0, 1, False, 0),
+        (a, (128, 64), 1, 1, True, 0),
+        (a, (128, 64), 2, 1, True, 1),
+        (a, (128, 64), 0, 0, False, 0),
+    ]
+    srv = octree_api.Server(lanes=1, memory_budget=64 << 30)
+    for case, grids, m, cid, dev, expect in steps:
+        want = alone(case, grids, m)
+        buf = buffers(want)
+        t = srv.submit(job_for(case, grids, m, *buf, device_bbox=dev, cloud_id=cid))
+        r = srv.wait(t)
+        srv.release(t)
+        check_same(want, r, *buf)
+        assert r.reused == expect, (grids, m, cid, dev)
+    srv.close()
