@@ -155,6 +155,24 @@ __device__ __forceinline__ float quant_units(int32_t q, const QAxis& a) {
     return __fmaf_rn(__fadd_rn((float)(q - a.qn), 0.5f), a.B, a.base);
 }
 
+// Position of the k-th set bit (k from 0) of m; k < popcount(m).
+__device__ __forceinline__ uint32_t nth_bit64(uint64_t m, uint32_t k) {
+    uint32_t pos = 0;
+#pragma unroll
+    for (uint32_t w = 32; w >= 1; w >>= 1) {
+        const uint64_t low = m & ((1ull << w) - 1ull);
+        const uint32_t c = (uint32_t)__popcll(low);
+        if (k >= c) {
+            k -= c;
+            m >>= w;
+            pos += w;
+        } else {
+            m = low;
+        }
+    }
+    return pos;
+}
+
 struct NodeShared {
     uint64_t start[8];
     uint32_t count[8];
@@ -495,14 +513,36 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
             if (threadIdx.x == 0) ns.cells = total;
         }
         sync_all();
-        // rank -> (brick slot, bit), for the per-cell emit
+        // rank -> (brick slot, bit), for the per-cell emit.  A warp lists the
+        // cells of its 32 consecutive slots (consecutive ranks) in rank order,
+        // 32 ranks per coalesced store: each lane finds the slot holding its
+        // rank by a search over the warp's running cell counts.
         for (uint32_t k = tid0; k < bm.cap; k += tstride) {
-            uint64_t m = bm.mask[k];
-            uint32_t r = bm.base[k];
-            while (m) {
-                const uint32_t bit = (uint32_t)__ffsll((long long)m) - 1;
-                m &= m - 1;
-                a.cell_slot[off + r++] = (k << 6) | bit;
+            const uint32_t lane = threadIdx.x & 31;
+            const uint64_t m = bm.mask[k];
+            const uint32_t c = (uint32_t)__popcll(m);
+            uint32_t incl = c;
+#pragma unroll
+            for (uint32_t o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += y;
+            }
+            const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+            const uint32_t base0 = __shfl_sync(0xffffffffu, bm.base[k], 0);
+            const uint32_t excl = incl - c;
+            for (uint32_t q0 = 0; q0 < total; q0 += 32) {
+                const uint32_t q = q0 + lane;
+                uint32_t lo = 0;
+#pragma unroll
+                for (uint32_t st = 16; st >= 1; st >>= 1) {
+                    const uint32_t v = __shfl_sync(0xffffffffu, incl, lo + st - 1);
+                    if (v <= q) lo += st;
+                }
+                const uint32_t ow = min(lo, 31u);
+                const uint64_t mo = ((uint64_t)__shfl_sync(0xffffffffu, (uint32_t)(m >> 32), ow) << 32) |
+                                    __shfl_sync(0xffffffffu, (uint32_t)m, ow);
+                const uint32_t eo = __shfl_sync(0xffffffffu, excl, ow);
+                if (q < total) a.cell_slot[off + base0 + q] = ((k - lane + ow) << 6) | nth_bit64(mo, q - eo);
             }
         }
         const uint32_t cells = ns0->cells;
