@@ -75,6 +75,24 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def replica_max(value, pg):
+    """The largest value over the ranks of the process group `pg` (the
+    torch.distributed module after init_process_group), or `value` alone."""
+    if not pg:
+        return value
+    import torch
+
+    t = torch.tensor([value], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replicas_throughput(points_per_rank, ranks, ms):
+    """Mpts/s of `ranks` independent replicas of a build of points_per_rank
+    points timed at `ms` (the slowest rank)."""
+    return points_per_rank * ranks / (ms * 1e-3) / 1e6
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -627,13 +645,8 @@ def main():
     clk = clocks.stop()
     st = s.stats()
     ms_step = statistics.mean(gen_ms)
-    if pg:
-        import torch
-
-        tt = torch.tensor([ms_step], dtype=torch.float64)
-        pg.all_reduce(tt, op=pg.ReduceOp.MAX)
-        ms_step = float(tt.item())
-    value = n * ws / (ms_step * 1e-3) / 1e6
+    ms_step = replica_max(ms_step, pg)
+    value = replicas_throughput(n, ws, ms_step)
     stage_avg = {k: v / args.steps for k, v in stage_sum.items()}
 
     # ---- end to end through the C ABI with host buffers
@@ -654,12 +667,7 @@ def main():
         octree_api._check(L.ocpi_get_records(s._h, recs.ctypes.data), "ocpi_get_records")
         e2e_times.append(time.perf_counter() - t0)
     e2e_s = statistics.median(e2e_times)
-    if pg:
-        import torch
-
-        tt = torch.tensor([e2e_s], dtype=torch.float64)
-        pg.all_reduce(tt, op=pg.ReduceOp.MAX)
-        e2e_s = float(tt.item())
+    e2e_s = replica_max(e2e_s, pg)
     upload_ms = None
     try:
         s.init()
