@@ -208,6 +208,20 @@ OCPI_EXPORT int ocpi_server_wait(void* server, uint64_t ticket, OcpiJobResult* r
 OCPI_EXPORT int ocpi_server_get_hierarchy(void* server, uint64_t ticket, uint8_t* out);
 /* forgets a completed job (waits for it first) */
 OCPI_EXPORT int ocpi_server_release(void* server, uint64_t ticket);
+/* a waiting job completes at once as failed ("cancelled"); -1 if it is running or done */
+OCPI_EXPORT int ocpi_server_cancel(void* server, uint64_t ticket);
+/* how many times a lane restarted after losing its worker */
+OCPI_EXPORT int ocpi_server_lane_restarts(void* server, uint64_t* restarts);
+
+/* Host-side fault injection for tests (no GPU fault is involved): the next
+ * `count` events of a kind fail.  OCPI_INJECT_ALLOCATION: a device or pinned
+ * allocation of any session or lane fails as if cudaMalloc had (the call
+ * returns -1, the job fails).  OCPI_INJECT_LANE_LOSS: a server lane that takes
+ * a job drops it and its state as if its worker had died, then restarts.
+ * count 0 clears a kind. */
+#define OCPI_INJECT_ALLOCATION 1
+#define OCPI_INJECT_LANE_LOSS 2
+OCPI_EXPORT int ocpi_debug_inject_failures(int kind, uint32_t count);
 /* all jobs submitted at once to an executor that the library keeps for the
  * rest of the process (one per device, lanes and budget), so that its lanes'
  * device buffers stay allocated between batches; returns -1 if any failed */

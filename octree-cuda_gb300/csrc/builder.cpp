@@ -7,6 +7,7 @@
 #include "builder.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -36,6 +37,26 @@ void BuildConfig::validate() const {
     if ((uint64_t)n * stride > (1ull << 40)) throw Error("cloud too large");
 }
 
+namespace {
+std::atomic<int32_t> g_injected[3];
+
+void allocation_hook() {
+    if (consume_injected_failure(kInjectAllocation)) throw Error("cudaMalloc failed: injected allocation failure");
+}
+}   // namespace
+
+void inject_failures(int kind, uint32_t count) {
+    if (kind != kInjectAllocation && kind != kInjectLaneLoss) throw Error("unknown fault kind");
+    g_injected[kind].store((int32_t)std::min<uint32_t>(count, 1u << 30));
+}
+
+bool consume_injected_failure(int kind) {
+    int32_t v = g_injected[kind].load();
+    while (v > 0)
+        if (g_injected[kind].compare_exchange_weak(v, v - 1)) return true;
+    return false;
+}
+
 DevBuf::~DevBuf() {
     release();
 }
@@ -48,6 +69,7 @@ void DevBuf::release() {
 
 void DevBuf::ensure(size_t b) {
     if (b <= bytes && p) return;
+    allocation_hook();
     release();
     size_t want = std::max<size_t>(b, 256);
     check_cuda(cudaMalloc(&p, want), "cudaMalloc");
@@ -56,6 +78,7 @@ void DevBuf::ensure(size_t b) {
 
 void DevBuf::ensure_keep(size_t b, size_t keep, cudaStream_t s) {
     if (b <= bytes && p) return;
+    allocation_hook();
     size_t want = std::max<size_t>(b + b / 4, 256);
     void* np = nullptr;
     check_cuda(cudaMalloc(&np, want), "cudaMalloc");
@@ -78,6 +101,7 @@ void HostBuf::release() {
 
 void HostBuf::ensure(size_t b) {
     if (b <= bytes && p) return;
+    allocation_hook();
     release();
     size_t want = std::max<size_t>(b + b / 4, 4096);
     check_cuda(cudaMallocHost(&p, want), "cudaMallocHost");

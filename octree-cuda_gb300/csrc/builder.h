@@ -122,6 +122,14 @@ MemoryTerms memory_terms(const BuildConfig& cfg, int num_sms);
 MemoryTerms envelope(const MemoryTerms& a, const MemoryTerms& b);
 uint64_t device_bytes(const MemoryTerms& t);
 
+// Host-side fault injection for tests: the next `count` events of a kind
+// fail.  Allocation: a device or pinned allocation throws as if cudaMalloc
+// had failed.  Lane loss: a server lane drops its job and state as if its
+// worker had died, and restarts.
+enum InjectKind : int { kInjectAllocation = 1, kInjectLaneLoss = 2 };
+void inject_failures(int kind, uint32_t count);
+bool consume_injected_failure(int kind);
+
 // Throws the message of the first error bit set in a device error word.
 void throw_device_errors(uint32_t e, const char* stage);
 

@@ -209,8 +209,15 @@ int ocpi_init_octree(void* session) {
             return;
         }
         if (s->builder) {
-            // another configuration: the same buffers, grown where needed
-            s->builder->reconfigure(s->cfg, s->host_cloud);
+            // another configuration: the same buffers, grown where needed.  A
+            // failure part-way (an allocation) leaves buffers sized for neither
+            // configuration, so the builder is dropped.
+            try {
+                s->builder->reconfigure(s->cfg, s->host_cloud);
+            } catch (...) {
+                s->builder.reset();
+                throw;
+            }
             if (s->out_rec) s->builder->set_output_host(s->out_rec, s->out_lut, s->out_cap);
             return;
         }

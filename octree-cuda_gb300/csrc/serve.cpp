@@ -179,6 +179,36 @@ public:
         std::memcpy(out, job->hierarchy.data(), job->hierarchy.size());
     }
 
+    // A waiting job leaves the queue and completes as failed ("cancelled");
+    // a running or completed job cannot be cancelled.
+    void cancel(uint64_t ticket) {
+        {
+            std::lock_guard<std::mutex> g(mu_);
+            auto it = jobs_.find(ticket);
+            if (it == jobs_.end()) throw Error("unknown ticket");
+            auto job = it->second;
+            if (job->done) throw Error("the job has already completed");
+            auto q = std::find(queue_.begin(), queue_.end(), job);
+            if (q == queue_.end()) throw Error("the job is running");
+            queue_.erase(q);
+            job->finished = Clock::now();
+            job->started = job->finished;
+            OcpiJobResult r{};
+            r.status = -1;
+            std::snprintf(r.error, sizeof r.error, "cancelled");
+            r.queuedMs = r.totalMs = ms_between(job->submitted, job->finished);
+            job->result = r;
+            job->done = true;
+        }
+        cv_done_.notify_all();
+        cv_work_.notify_all();
+    }
+
+    uint64_t lane_restarts() {
+        std::lock_guard<std::mutex> g(mu_);
+        return lane_restarts_;
+    }
+
     void release(uint64_t ticket) {
         std::unique_lock<std::mutex> g(mu_);
         auto it = jobs_.find(ticket);
@@ -243,8 +273,49 @@ private:
         return false;
     }
 
+    // A lane's worker.  A lost worker (simulated on the host: an exception
+    // outside any job) has already failed its job and dropped its state; the
+    // lane restarts with an empty builder.
     void run_lane(uint32_t l) {
         cudaSetDevice(device_);
+        for (;;) {
+            try {
+                lane_loop(l);
+                return;
+            } catch (const LaneLost&) {
+                // counted in fail_taken, before the job's waiter wakes
+            }
+        }
+    }
+
+    struct LaneLost {};
+
+    // Fails a job that was taken but not built, its worker lost (mutex not
+    // held); the lane's restart is counted here.
+    void fail_taken(uint32_t l, const std::shared_ptr<Job>& job, const char* why) {
+        {
+            std::lock_guard<std::mutex> g(mu_);
+            ++lane_restarts_;
+            job->finished = Clock::now();
+            OcpiJobResult r{};
+            r.status = -1;
+            std::snprintf(r.error, sizeof r.error, "%s", why);
+            r.lane = l;
+            r.queuedMs = ms_between(job->submitted, job->started);
+            r.runMs = ms_between(job->started, job->finished);
+            r.totalMs = ms_between(job->submitted, job->finished);
+            job->result = r;
+            job->done = true;
+            busy_[l] = false;
+            reserved_[l] = 0;
+            env_[l] = MemoryTerms{};
+            resident_[l] = 0;
+        }
+        cv_done_.notify_all();
+        cv_work_.notify_all();
+    }
+
+    void lane_loop(uint32_t l) {
         std::unique_ptr<Builder> builder;
         for (;;) {
             std::shared_ptr<Job> job;
@@ -276,6 +347,11 @@ private:
                 }
                 cv_work_.notify_all();
                 continue;
+            }
+            if (consume_injected_failure(kInjectLaneLoss)) {
+                builder.reset();
+                fail_taken(l, job, "worker lost; the lane restarted");
+                throw LaneLost{};
             }
             OcpiJobResult r{};
             std::vector<uint8_t> hier;
@@ -360,6 +436,7 @@ private:
     std::vector<bool> busy_, releasing_;
     std::vector<std::thread> workers_;
     uint64_t next_ticket_ = 0;
+    uint64_t lane_restarts_ = 0;
     bool stop_ = false;
 };
 
@@ -428,6 +505,21 @@ int ocpi_server_get_hierarchy(void* server, uint64_t ticket, uint8_t* out) {
         if (!out) throw oc::Error("null output");
         oc::to_executor(server)->hierarchy(ticket, out);
     });
+}
+
+int ocpi_server_cancel(void* server, uint64_t ticket) {
+    return oc::guarded([&] { oc::to_executor(server)->cancel(ticket); });
+}
+
+int ocpi_server_lane_restarts(void* server, uint64_t* restarts) {
+    return oc::guarded([&] {
+        if (!restarts) throw oc::Error("null output");
+        *restarts = oc::to_executor(server)->lane_restarts();
+    });
+}
+
+int ocpi_debug_inject_failures(int kind, uint32_t count) {
+    return oc::guarded([&] { oc::inject_failures(kind, count); });
 }
 
 int ocpi_server_release(void* server, uint64_t ticket) {

@@ -32,7 +32,8 @@ ADDED_SYMBOLS = [
     "ocpi_get_level_counts", "ocpi_get_timings", "ocpi_subsample_node_noalloc", "ocpi_set_output_host",
     "ocpi_compute_cloud_bb", "ocpi_get_device_memory", "ocpi_estimate_memory",
     "ocpi_server_create", "ocpi_server_destroy", "ocpi_server_submit", "ocpi_server_wait",
-    "ocpi_server_get_hierarchy", "ocpi_server_release", "ocpi_batch_build",
+    "ocpi_server_get_hierarchy", "ocpi_server_release", "ocpi_batch_build", "ocpi_server_cancel",
+    "ocpi_server_lane_restarts", "ocpi_debug_inject_failures",
 ]
 
 HIER_DTYPE = np.dtype([("type", "u1"), ("mask", "u1"), ("points", "<u4"),
@@ -136,6 +137,9 @@ def load_library(path=LIB_PATH):
         "ocpi_server_wait": [vp, u64, ctypes.POINTER(OcpiJobResult)],
         "ocpi_server_get_hierarchy": [vp, u64, vp],
         "ocpi_server_release": [vp, u64],
+        "ocpi_server_cancel": [vp, u64],
+        "ocpi_server_lane_restarts": [vp, ctypes.POINTER(u64)],
+        "ocpi_debug_inject_failures": [ctypes.c_int, u32],
         "ocpi_batch_build": [ctypes.c_int, u32, u64, ctypes.POINTER(OcpiJob), u32, ctypes.POINTER(OcpiJobResult)],
         "ocpi_estimate_memory": [u32, u32, u8, u32, u32, ctypes.c_float, u32, u32, ctypes.POINTER(u64),
                                  ctypes.POINTER(u64)],
@@ -399,6 +403,14 @@ class Server:
     def release(self, ticket):
         _check(load_library().ocpi_server_release(self._h, ticket), "ocpi_server_release")
 
+    def cancel(self, ticket):
+        _check(load_library().ocpi_server_cancel(self._h, ticket), "ocpi_server_cancel")
+
+    def lane_restarts(self):
+        v = ctypes.c_uint64()
+        _check(load_library().ocpi_server_lane_restarts(self._h, ctypes.byref(v)), "ocpi_server_lane_restarts")
+        return v.value
+
     def close(self):
         if self._h:
             load_library().ocpi_server_destroy(self._h)
@@ -409,6 +421,15 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+INJECT_ALLOCATION, INJECT_LANE_LOSS = 1, 2
+
+
+def inject_failures(kind, count):
+    """Host-side fault injection for tests: the next `count` events of a kind
+    (INJECT_ALLOCATION, INJECT_LANE_LOSS) fail; 0 clears."""
+    _check(load_library().ocpi_debug_inject_failures(kind, count), "ocpi_debug_inject_failures")
 
 
 def batch_build(jobs, device=0, lanes=4, memory_budget=150 << 30):

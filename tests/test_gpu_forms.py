@@ -148,3 +148,108 @@ def test_server_reuses_resident_cloud_state():
         check_same(want, r, *buf)
         assert r.reused == expect, (grids, m, cid, dev)
     srv.close()
+
+
+def test_injected_allocation_failure_fails_one_job_only():
+    case = make_case(0, 0, 200_000, seed=61)
+    want = alone(case, (128, 64), 0)
+    srv = octree_api.Server(lanes=1, memory_budget=64 << 30)
+    try:
+        octree_api.inject_failures(octree_api.INJECT_ALLOCATION, 1)
+        buf = buffers(want)
+        t = srv.submit(job_for(case, (128, 64), 0, *buf))
+        r = srv.wait(t)
+        srv.release(t)
+        assert r.status == -1 and b"injected allocation failure" in r.error
+        buf = buffers(want)
+        t = srv.submit(job_for(case, (128, 64), 0, *buf))
+        r = srv.wait(t)
+        srv.release(t)
+        check_same(want, r, *buf)
+    finally:
+        octree_api.inject_failures(octree_api.INJECT_ALLOCATION, 0)
+        srv.close()
+
+
+def test_injected_allocation_failure_in_a_session():
+    """A session whose reconfiguration fails part-way drops its builder; the
+    next ocpi_init_octree starts over and the build is correct."""
+    a = make_case(0, 0, 150_000, seed=62)
+    b = make_case(1, 0, 400_000, seed=63)
+    want = alone(b, (128, 64), 0)
+    s = octree_api.OctreeSession(0)
+    try:
+        cfg = dict(chunk_grid=64, sub_grid=32, merge_threshold=2000, seed=99, **MODES[0])
+        s.set_cloud(a.cloud, n=a.n, stride=a.stride, cloud_type=a.cloud_type, scale=a.scale, bb_min=a.bb_min,
+                    bb_max=a.bb_max)
+        s.configure(**cfg)
+        s.init()
+        s.generate()
+        # a larger cloud and grid: the buffers must grow, and the first growth fails
+        cfg = dict(chunk_grid=128, sub_grid=64, merge_threshold=2000, seed=99, **MODES[0])
+        s.set_cloud(b.cloud, n=b.n, stride=b.stride, cloud_type=b.cloud_type, scale=b.scale, bb_min=b.bb_min,
+                    bb_max=b.bb_max)
+        s.configure(**cfg)
+        octree_api.inject_failures(octree_api.INJECT_ALLOCATION, 1)
+        with pytest.raises(octree_api.OctreeError, match="injected allocation failure"):
+            s.init()
+        s.init()
+        s.generate()
+        a_r, a_l = node_sorted(want[0], want[1], want[2])
+        h = s.hierarchy()
+        assert h.tobytes() == want[0].tobytes()
+        b_r, b_l = node_sorted(h, s.records(), s.lut())
+        assert np.array_equal(a_l, b_l) and a_r.tobytes() == b_r.tobytes()
+    finally:
+        octree_api.inject_failures(octree_api.INJECT_ALLOCATION, 0)
+        s.close()
+
+
+def test_lane_restarts_after_losing_its_worker():
+    case = make_case(2, 1, 200_000, seed=64)
+    want = alone(case, (128, 64), 0)
+    srv = octree_api.Server(lanes=2, memory_budget=64 << 30)
+    try:
+        octree_api.inject_failures(octree_api.INJECT_LANE_LOSS, 1)
+        buf = buffers(want)
+        t = srv.submit(job_for(case, (128, 64), 0, *buf))
+        r = srv.wait(t)
+        srv.release(t)
+        assert r.status == -1 and b"worker lost" in r.error
+        assert srv.lane_restarts() == 1
+        results = []
+        for _ in range(4):   # both lanes serve again
+            buf = buffers(want)
+            t = srv.submit(job_for(case, (128, 64), 0, *buf))
+            results.append((srv.wait(t), buf))
+            srv.release(t)
+        for r, buf in results:
+            check_same(want, r, *buf)
+    finally:
+        octree_api.inject_failures(octree_api.INJECT_LANE_LOSS, 0)
+        srv.close()
+
+
+def test_cancel_a_waiting_job():
+    """A budget that holds one job at a time: the second job waits behind the
+    first and can be cancelled; the running one cannot."""
+    big = make_case(0, 0, 3_000_000, seed=65)
+    small = make_case(1, 0, 100_000, seed=66)
+    want_big = alone(big, (128, 64), 0)
+    bound = octree_api.estimate_memory(big.n, big.stride, big.cloud_type, 128, 2000, 2.2, 64, FLAGS[0])[0]
+    srv = octree_api.Server(lanes=2, memory_budget=int(bound * 1.05))
+    try:
+        buf = buffers(want_big)
+        t1 = srv.submit(job_for(big, (128, 64), 0, *buf))
+        t2 = srv.submit(job_for(small, (128, 64), 0, None, None, None))
+        srv.cancel(t2)
+        r2 = srv.wait(t2)
+        assert r2.status == -1 and r2.error == b"cancelled"
+        with pytest.raises(octree_api.OctreeError, match="completed"):
+            srv.cancel(t2)
+        r1 = srv.wait(t1)
+        check_same(want_big, r1, *buf)
+        with pytest.raises(octree_api.OctreeError, match="completed"):
+            srv.cancel(t1)
+    finally:
+        srv.close()

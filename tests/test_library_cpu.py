@@ -119,3 +119,11 @@ def test_job_structs_match_the_header(tmp_path):
         want.append(ctypes.sizeof(st))
         want += [getattr(st, f).offset for f, _ in st._fields_]
     assert got == want
+
+
+def test_fault_injection_kinds():
+    L = octree_api.load_library()
+    assert L.ocpi_debug_inject_failures(7, 1) == -1
+    assert b"unknown fault kind" in L.ocpi_last_error()
+    assert L.ocpi_debug_inject_failures(octree_api.INJECT_ALLOCATION, 0) == 0
+    assert L.ocpi_debug_inject_failures(octree_api.INJECT_LANE_LOSS, 0) == 0
