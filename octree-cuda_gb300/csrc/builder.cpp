@@ -315,6 +315,7 @@ void Builder::fill_cell_tables() {
 // calculateRealBB + calculateCubicBB (src/boundingbox.h:11-52) over the
 // uploaded cloud; the cubic box becomes the build's bounding box.
 void Builder::compute_bbox(double real[6], double cubic[6]) {
+    TraceRange trace("bounding box");
     tree_valid_ = false;
     reuse_tree_ = false;
     bbox_keys_.ensure(6 * 8);
@@ -556,6 +557,7 @@ void Builder::set_output_host(uint8_t* records, uint32_t* lut, uint64_t capacity
 }
 
 void Builder::upload(const uint8_t* host_cloud, bool wait) {
+    TraceRange trace("upload");
     if (!host_cloud) throw Error("no point cloud set");
     tree_valid_ = false;
     reuse_tree_ = false;
@@ -590,6 +592,7 @@ void throw_device_errors(uint32_t e, const char* stage) {
 }
 
 void Builder::generate() {
+    TraceRange trace(reuse_tree_ ? "generate (resident tree)" : "generate");
     host_filled_ = false;
     sub_err_valid_ = false;
     if (reuse_tree_) {
@@ -693,6 +696,7 @@ void Builder::generate() {
 // Host copy of the node table (NodeHost), read on the side stream once tree
 // enumeration is done, while distribution runs on the build stream.
 void Builder::build_tree_host() {
+    TraceRange trace("node table");
     check_cuda(cudaStreamWaitEvent(side_stream_, tree_ready_, 0), "wait");
     tree_host_.ensure(64);
     check_cuda(cudaMemcpyAsync(tree_host_.as<uint32_t>(0), n_nodes_.p, 4, cudaMemcpyDeviceToHost, side_stream_), "D2H");
@@ -774,6 +778,7 @@ void Builder::build_tree_host() {
 }
 
 void Builder::subsample() {
+    TraceRange trace("subsample");
     const double cubic = cfg_.bb_max[0] - cfg_.bb_min[0];
     const uint32_t S = cfg_.sub_grid;
     uint32_t mode = 0;

@@ -13,7 +13,18 @@
 
 #include "kernels.h"
 
+#include <nvtx3/nvToolsExt.h>
+
 namespace oc {
+
+// A named NVTX range for the lifetime of the object (host phases of a build
+// on a profiler's timeline; nearly free when no tool is attached).
+struct TraceRange {
+    explicit TraceRange(const char* name) { nvtxRangePushA(name); }
+    ~TraceRange() { nvtxRangePop(); }
+    TraceRange(const TraceRange&) = delete;
+    TraceRange& operator=(const TraceRange&) = delete;
+};
 
 struct Error : std::runtime_error {
     using std::runtime_error::runtime_error;

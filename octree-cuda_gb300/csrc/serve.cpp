@@ -356,6 +356,7 @@ private:
             OcpiJobResult r{};
             std::vector<uint8_t> hier;
             try {
+                TraceRange trace("job");
                 const OcpiJob& s = job->spec;
                 BuildConfig cfg = job->cfg;
                 const bool device_bb = !cfg.has_bbox();
