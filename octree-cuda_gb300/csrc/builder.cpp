@@ -262,7 +262,15 @@ void Builder::size_for_config() {
     }
     node_cap_ = (uint32_t)std::min<uint64_t>(cap, level_off_[depth_ + 1]);
 
-    pyr_.ensure(level_off_[depth_ + 1] * 4);
+    {
+        // a new pyramid or bitmap allocation holds garbage: the next build
+        // clears it in full
+        const void* old_pyr = pyr_.p;
+        const void* old_occ = occ_.p;
+        pyr_.ensure(level_off_[depth_ + 1] * 4);
+        occ_.ensure(std::max<uint64_t>(level_off_[1] >> 6, 1));
+        if (pyr_.p != old_pyr || occ_.p != old_occ) pyr_zero_ = false;
+    }
     loff_.ensure(level_off_.size() * 8);
     params_writable();
     loff_host_.ensure(level_off_.size() * 8);
@@ -422,7 +430,7 @@ void Builder::collect_timings() {
 std::vector<std::pair<std::string, uint64_t>> Builder::device_allocations() const {
     return {
         {"cloud", cloud_.bytes},
-        {"count pyramid", pyr_.bytes},
+        {"count pyramid", pyr_.bytes + occ_.bytes},
         {"node table", key_.bytes + count_.bytes + level_.bytes + info_.bytes + child_first_.bytes +
                            data_idx_.bytes + fill_.bytes + level_start_.bytes + n_nodes_.bytes + loff_.bytes +
                            nonzero_.bytes},
@@ -502,6 +510,7 @@ uint64_t device_bytes(const MemoryTerms& t) {
     uint64_t b = 0;
     b += t.cloud_bytes + 64;                                           // cloud
     b += t.cells * 4;                                                  // count pyramid
+    b += t.cells / 64 + 1;                                             // occupancy flags of finest-level blocks
     b += t.node_cap * (4 + 4 + 1 + 2 + 4 + 4 + 8 + 4);                 // node table, leaf lists, fill
     b += t.out_cap * (4 + 18) + 16;                                    // final LUT + records
     b += t.out_cap * (4 + 18 + 4) + 64;                                // staged LUT + records + sub-step words
@@ -630,16 +639,30 @@ void Builder::generate() {
     for (int a = 0; a < 3; ++a) op.ax[a] = make_out_axis(cfg_.bb_min[a], 1.0 / cfg_.scale[a]);   // octree_chunking.cu:109-111
     const bool f32 = cfg_.cloud_type == 0;
 
+    // Sparse clouds (at most one point per 16 finest cells) flag the 64-cell
+    // blocks of the finest level they touch (one byte per block): counting
+    // sets the flags, the pyramid and the tag push skip unflagged blocks, and
+    // the build ends by zeroing only the flagged blocks and the upper levels,
+    // so the next build finds the pyramid zero.  Denser clouds clear the
+    // whole pyramid first.
+    const uint64_t cells0 = level_off_[1];
+    const bool sparse = depth_ >= 2 && (uint64_t)cfg_.n * 16 <= cells0;
+    const uint64_t occ_blocks = cells0 >> 6;
+    uint8_t* occ = sparse ? occ_.as<uint8_t>() : nullptr;
     stage_begin();
-    check_cuda(cudaMemsetAsync(pyr_.p, 0, level_off_[depth_ + 1] * 4, stream_), "memset");
+    if (!sparse || !pyr_zero_) {
+        check_cuda(cudaMemsetAsync(pyr_.p, 0, level_off_[depth_ + 1] * 4, stream_), "memset");
+        if (sparse) check_cuda(cudaMemsetAsync(occ_.p, 0, occ_blocks, stream_), "memset");
+    }
+    pyr_zero_ = false;
     check_cuda(cudaMemsetAsync(err_.p, 0, 64, stream_), "memset");
     check_cuda(cudaMemsetAsync(nonzero_.p, 0, (depth_ + 1) * 4, stream_), "memset");
     stage_mark("clear");
     launches_ = 0;
-    launches_ += launch_count(cloud_.as<uint8_t>(), cfg_.n, cfg_.stride, f32, g, pyr_.as<uint32_t>(),
+    launches_ += launch_count(cloud_.as<uint8_t>(), cfg_.n, cfg_.stride, f32, g, pyr_.as<uint32_t>(), occ,
                               err_.as<uint32_t>(), num_sms_, stream_);
     stage_mark("count");
-    launches_ += launch_pyramid(pyr_.as<uint32_t>(), level_off_.data(), depth_, nonzero_.as<uint32_t>(), stream_);
+    launches_ += launch_pyramid(pyr_.as<uint32_t>(), level_off_.data(), depth_, nonzero_.as<uint32_t>(), occ, stream_);
     stage_mark("pyramid");
     launches_ += launch_enumerate(pyr_.as<uint32_t>(), loff_.as<uint64_t>(), depth_, cfg_.threshold, key_.as<uint32_t>(),
                      count_.as<uint32_t>(), level_.as<uint8_t>(), info_.as<uint16_t>(), child_first_.as<uint32_t>(),
@@ -672,7 +695,7 @@ void Builder::generate() {
     launches_ += launch_leaf_prep(n_nodes_.as<uint32_t>(), info_.as<uint16_t>(), count_.as<uint32_t>(),
                                   level_.as<uint8_t>(), key_.as<uint32_t>(), pyr_.as<uint32_t>(), loff_.as<uint64_t>(),
                                   data_idx_.as<uint64_t>(), fill_.as<uint32_t>(), cfg_.n, err_.as<uint32_t>(), stream_);
-    launches_ += launch_push_tags(pyr_.as<uint32_t>(), loff_.as<uint64_t>(), depth_, cfg_.chunk_grid,
+    launches_ += launch_push_tags(pyr_.as<uint32_t>(), loff_.as<uint64_t>(), depth_, cfg_.chunk_grid, occ,
                                   err_.as<uint32_t>(), stream_);
     launches_ += launch_distribute(cloud_.as<uint8_t>(), cfg_.n, cfg_.stride, f32, g, op, pyr_.as<uint32_t>(),
                                    data_idx_.as<uint64_t>(), fill_.as<uint32_t>(), lut_.as<uint32_t>(),
@@ -688,6 +711,14 @@ void Builder::generate() {
     // subsampling
     if (sub_err_valid_) throw_device_errors(sub_err_, "generate");
     else check_device_errors("generate");
+    if (sparse) {
+        launches_ += launch_sparse_zero(pyr_.as<uint32_t>(), occ, occ_blocks, stream_);
+        check_cuda(cudaMemsetAsync(pyr_.as<uint32_t>() + cells0, 0, (level_off_[depth_ + 1] - cells0) * 4, stream_),
+                   "memset");
+        stage_mark("cleanup");
+        check_cuda(cudaStreamSynchronize(stream_), "cleanup");
+        pyr_zero_ = true;
+    }
     collect_timings();
     compute_stats();
     tree_valid_ = true;

@@ -214,6 +214,8 @@ private:
     uint32_t node_cap_ = 0;
 
     DevBuf cloud_, pyr_, loff_, err_, nonzero_;
+    DevBuf occ_;                        // sparse clouds: one flag byte per 64-cell block of the finest level
+    bool pyr_zero_ = false;             // the pyramid and the flags are all zero (sparse clean-up ran)
     DevBuf key_, count_, level_, info_, child_first_, level_start_, n_nodes_;
     DevBuf data_idx_, fill_;
     DevBuf lut_, rec_;                  // final outputs (N + P_out records)

@@ -185,9 +185,12 @@ __device__ __forceinline__ uint32_t cell_morton(const int cell[3], const uint8_t
 
 // K1 (point_counting.cuh:29-53): points per finest cell.  Consecutive lanes
 // in the same cell add their count with one atomic.
+// With `occ` (sparse clouds) the run leaders also flag their cell's 64-cell
+// block (a level-2 cell): a plain byte store, no read-modify-write.
 template <bool kF32>
 __global__ void __launch_bounds__(kCountThreads) k_count(const uint8_t* __restrict__ cloud, uint64_t n, uint32_t stride,
-                                                         CloudGrid g, uint32_t* __restrict__ pyr0, uint32_t* err) {
+                                                         CloudGrid g, uint32_t* __restrict__ pyr0, uint8_t* occ,
+                                                         uint32_t* err) {
     extern __shared__ __align__(128) uint8_t smem[];
     const ChunkSmem L = chunk_smem(stride, g.grid, kF32, kCountTile, 0);
     load_tables<kF32>(g, smem, L);
@@ -206,7 +209,10 @@ __global__ void __launch_bounds__(kCountThreads) k_count(const uint8_t* __restri
                 else set_error(err, kErrBelowBox);
             }
             const uint32_t starts = run_starts(m);
-            if (m != kNoKey && ((starts >> lane) & 1u)) atomicAdd(&pyr0[m], run_end(starts) - lane);
+            if (m != kNoKey && ((starts >> lane) & 1u)) {
+                atomicAdd(&pyr0[m], run_end(starts) - lane);
+                if (occ) occ[m >> 6] = 1;
+            }
         }
     });
 }
@@ -267,11 +273,20 @@ __global__ void k_bbox_init(long long* keys) {
 
 // Level l -> levels l+1 and l+2: one thread per level-(l+2) cell reads its 64
 // Morton-contiguous level-l counts.
+// With `occ` (the finest level of a sparse cloud), a level-2 cell whose
+// block flag is clear has only empty children: its sums are written as 0
+// without reading them.
 __global__ void k_pyramid2(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst1, uint32_t* __restrict__ dst2,
-                           uint64_t n2, uint32_t* nz_src, uint32_t* nz_dst1) {
+                           uint64_t n2, uint32_t* nz_src, uint32_t* nz_dst1, const uint8_t* __restrict__ occ) {
     uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     uint32_t nzs = 0, nzd = 0;
-    if (i < n2) {
+    const bool empty = i < n2 && occ && occ[i] == 0;
+    if (empty) {
+        uint4* d = reinterpret_cast<uint4*>(dst1 + i * 8);
+        d[0] = make_uint4(0, 0, 0, 0);
+        d[1] = make_uint4(0, 0, 0, 0);
+        dst2[i] = 0;
+    } else if (i < n2) {
         const uint4* s = reinterpret_cast<const uint4*>(src + i * 64);
         uint32_t sums[8];
         uint32_t total = 0;
@@ -459,9 +474,10 @@ __global__ void __launch_bounds__(1024) k_leaf_prep(const uint32_t* __restrict__
 // thread per level-1 cell reads its 8 children and, when some of them are
 // occupied and untagged, the nearest tagged ancestor.
 __global__ void k_push_tags(uint32_t* __restrict__ pyr, const uint64_t* __restrict__ loff, uint32_t depth, uint64_t n1,
-                            uint32_t* err) {
+                            const uint8_t* __restrict__ occ, uint32_t* err) {
     const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (i >= n1) return;
+    if (occ && occ[i >> 3] == 0) return;   // no point in this 64-cell block
     uint4* c = reinterpret_cast<uint4*>(pyr + i * 8);
     uint4 a = c[0], b = c[1];
     uint32_t v[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
@@ -706,20 +722,38 @@ static int chunk_grid_size(Kernel kernel, uint32_t threads, uint32_t tile, size_
 }
 
 int launch_count(const uint8_t* cloud, uint64_t n, uint32_t stride, bool float_input, const CloudGrid& g,
-                  uint32_t* pyr0, uint32_t* err, int num_sms, cudaStream_t stream) {
+                  uint32_t* pyr0, uint8_t* occ, uint32_t* err, int num_sms, cudaStream_t stream) {
     if (n == 0) return 0;
     const size_t smem = chunk_smem(stride, g.grid, float_input, kCountTile, 0).total;
     if (float_input) {
         const int grid = chunk_grid_size(k_count<true>, kCountThreads, kCountTile, smem, n, num_sms);
-        k_count<true><<<grid, kCountThreads, smem, stream>>>(cloud, n, stride, g, pyr0, err);
+        k_count<true><<<grid, kCountThreads, smem, stream>>>(cloud, n, stride, g, pyr0, occ, err);
     } else {
         const int grid = chunk_grid_size(k_count<false>, kCountThreads, kCountTile, smem, n, num_sms);
-        k_count<false><<<grid, kCountThreads, smem, stream>>>(cloud, n, stride, g, pyr0, err);
+        k_count<false><<<grid, kCountThreads, smem, stream>>>(cloud, n, stride, g, pyr0, occ, err);
     }
     return 1;
 }
 
-int launch_pyramid(uint32_t* pyr, const uint64_t* loff, uint32_t depth, uint32_t* nonzero, cudaStream_t stream) {
+// Zeroes the 64-cell blocks of the finest level flagged in `occ`, and the
+// flags: one thread per block.
+__global__ void k_sparse_zero(uint32_t* __restrict__ pyr0, uint8_t* __restrict__ occ, uint64_t blocks) {
+    const uint64_t b = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (b >= blocks || !occ[b]) return;
+    uint4* d = reinterpret_cast<uint4*>(pyr0 + b * 64);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) d[k] = make_uint4(0, 0, 0, 0);
+    occ[b] = 0;
+}
+
+int launch_sparse_zero(uint32_t* pyr0, uint8_t* occ, uint64_t blocks, cudaStream_t stream) {
+    if (!blocks) return 0;
+    k_sparse_zero<<<(unsigned)((blocks + 255) / 256), 256, 0, stream>>>(pyr0, occ, blocks);
+    return 1;
+}
+
+int launch_pyramid(uint32_t* pyr, const uint64_t* loff, uint32_t depth, uint32_t* nonzero, const uint8_t* occ,
+                   cudaStream_t stream) {
     uint32_t l = 0;
     int launches = 1;
     while (l < depth) {
@@ -732,7 +766,8 @@ int launch_pyramid(uint32_t* pyr, const uint64_t* loff, uint32_t depth, uint32_t
             int threads = 256;
             uint64_t blocks = (n2 + threads - 1) / threads;
             k_pyramid2<<<(unsigned)blocks, threads, 0, stream>>>(pyr + loff[l], pyr + loff[l + 1], pyr + loff[l + 2],
-                                                                 n2, nonzero + l, nonzero + l + 1);
+                                                                 n2, nonzero + l, nonzero + l + 1,
+                                                                 l == 0 ? occ : nullptr);
             l += 2;
         } else {
             uint64_t n1 = loff[l + 2] - loff[l + 1];
@@ -771,11 +806,11 @@ int launch_leaf_prep(const uint32_t* n_nodes, const uint16_t* info, const uint32
     return 1;
 }
 
-int launch_push_tags(uint32_t* pyr, const uint64_t* loff_dev, uint32_t depth, uint32_t grid, uint32_t* err,
-                     cudaStream_t stream) {
+int launch_push_tags(uint32_t* pyr, const uint64_t* loff_dev, uint32_t depth, uint32_t grid, const uint8_t* occ,
+                     uint32_t* err, cudaStream_t stream) {
     const uint64_t n1 = (uint64_t)(grid / 2) * (grid / 2) * (grid / 2);
     if (!n1) return 0;
-    k_push_tags<<<(unsigned)((n1 + 255) / 256), 256, 0, stream>>>(pyr, loff_dev, depth, n1, err);
+    k_push_tags<<<(unsigned)((n1 + 255) / 256), 256, 0, stream>>>(pyr, loff_dev, depth, n1, occ, err);
     return 1;
 }
 

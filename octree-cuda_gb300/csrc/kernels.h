@@ -123,13 +123,21 @@ struct SubLevelArgs {
     uint32_t global_shift;   // 32 - log2(global_cap)
 };
 
+// Points per finest cell.  occ != nullptr (sparse clouds): also flags, one
+// byte per 64-cell block of the finest level (a level-2 cell), the blocks
+// that received points.
 int launch_count(const uint8_t* cloud, uint64_t n, uint32_t stride, bool float_input, const CloudGrid& g,
-                  uint32_t* pyr0, uint32_t* err, int num_sms, cudaStream_t stream);
+                  uint32_t* pyr0, uint8_t* occ, uint32_t* err, int num_sms, cudaStream_t stream);
+
+// Zeroes the finest-level blocks flagged in `occ` (`blocks` flags) and the
+// flags themselves.
+int launch_sparse_zero(uint32_t* pyr0, uint8_t* occ, uint64_t blocks, cudaStream_t stream);
 
 // Builds levels 1..depth of the Morton count pyramid from level 0 and counts
-// occupied cells per level into `nonzero[level]`.
+// occupied cells per level into `nonzero[level]`.  With occ, finest-level
+// blocks whose bit is clear are not read.
 int launch_pyramid(uint32_t* pyr, const uint64_t* level_off_host, uint32_t depth, uint32_t* nonzero,
-                    cudaStream_t stream);
+                    const uint8_t* occ, cudaStream_t stream);
 
 int launch_enumerate(const uint32_t* pyr, const uint64_t* level_off_dev, uint32_t depth, uint32_t threshold,
                       uint32_t* key, uint32_t* count, uint8_t* level, uint16_t* info, uint32_t* child_first,
@@ -149,8 +157,8 @@ int launch_leaf_prep(const uint32_t* n_nodes, const uint16_t* info, const uint32
 
 // Writes each occupied finest-level cell's leaf tag into the cell (after
 // launch_leaf_prep), so that distribution finds a point's leaf in one read.
-int launch_push_tags(uint32_t* pyr, const uint64_t* level_off_dev, uint32_t depth, uint32_t grid, uint32_t* err,
-                     cudaStream_t stream);
+int launch_push_tags(uint32_t* pyr, const uint64_t* level_off_dev, uint32_t depth, uint32_t grid, const uint8_t* occ,
+                     uint32_t* err, cudaStream_t stream);
 
 int launch_distribute(const uint8_t* cloud, uint64_t n, uint32_t stride, bool float_input, const CloudGrid& g,
                       const OutParams& out, const uint32_t* pyr0, const uint64_t* data_idx, uint32_t* fill,
