@@ -658,22 +658,22 @@ def main():
     recs = pinned_bytes(max(int(np.float32(n) * np.float32(CFG["output_factor"])), st["points_total"]) * 18)
     s.set_output_host(recs)
     L = octree_api.load_library()
+    init_times = []
     for i in range(max(2, min(args.steps, 3))):
         barrier()
         t0 = time.perf_counter()
         s.init()
+        init_times.append(time.perf_counter() - t0)
         s.generate()
         h = s.hierarchy()
         octree_api._check(L.ocpi_get_records(s._h, recs.ctypes.data), "ocpi_get_records")
         e2e_times.append(time.perf_counter() - t0)
     e2e_s = statistics.median(e2e_times)
     e2e_s = replica_max(e2e_s, pg)
-    upload_ms = None
-    try:
-        s.init()
-        upload_ms = s.timings().get("upload")
-    except Exception:
-        pass
+    # ocpi_init_octree inside the end-to-end steps: the chunked upload, with
+    # the cloud binned as its chunks land (the call returns when the copy is
+    # done)
+    upload_ms = round(statistics.median(init_times) * 1e3, 3)
 
     # ---- roofline of the dominant stage
     peak, peak_kind = peaks()

@@ -205,7 +205,8 @@ void make_cell_keys32(double mn, double t, uint32_t grid, int32_t* keys) {
     keys[grid] = keys[grid + 1] = INT32_MAX;
 }
 
-Builder::Builder(const BuildConfig& cfg, const uint8_t* host_cloud, int device) : cfg_(cfg), device_(device) {
+Builder::Builder(const BuildConfig& cfg, const uint8_t* host_cloud, int device, bool count)
+    : cfg_(cfg), device_(device) {
     cfg_.validate();
     check_cuda(cudaSetDevice(device_), "cudaSetDevice");
     check_cuda(cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, device_), "device attribute");
@@ -214,12 +215,12 @@ Builder::Builder(const BuildConfig& cfg, const uint8_t* host_cloud, int device) 
     check_cuda(cudaEventCreateWithFlags(&tree_ready_, cudaEventDisableTiming), "event");
     check_cuda(cudaEventCreateWithFlags(&params_done_, cudaEventDisableTiming), "event");
     size_for_config();
-    upload(host_cloud);
+    upload(host_cloud, true, count);
 }
 
 // A new cloud and configuration on the same device state: every buffer only
 // grows, so a builder that has served larger builds allocates nothing.
-void Builder::reconfigure(const BuildConfig& cfg, const uint8_t* host_cloud, bool wait_upload) {
+void Builder::reconfigure(const BuildConfig& cfg, const uint8_t* host_cloud, bool wait_upload, bool count) {
     cfg.validate();
     tree_valid_ = false;
     reuse_tree_ = false;
@@ -233,7 +234,7 @@ void Builder::reconfigure(const BuildConfig& cfg, const uint8_t* host_cloud, boo
     nodes_.clear();
     stats_ = Stats{};
     size_for_config();
-    upload(host_cloud, wait_upload);
+    upload(host_cloud, wait_upload, count);
 }
 
 // The staged parameter tables may be rewritten once their last upload is done.
@@ -325,6 +326,7 @@ void Builder::fill_cell_tables() {
 void Builder::compute_bbox(double real[6], double cubic[6]) {
     TraceRange trace("bounding box");
     tree_valid_ = false;
+    counted_ = false;   // the box changes: any counts of an overlapped upload are void
     reuse_tree_ = false;
     bbox_keys_.ensure(6 * 8);
     launches_ = 0;
@@ -395,6 +397,7 @@ Builder::~Builder() {
     if (tree_ready_) cudaEventDestroy(tree_ready_);
     if (side_stream_) cudaStreamDestroy(side_stream_);
     if (params_done_) cudaEventDestroy(params_done_);
+    for (auto e : chunk_ready_) cudaEventDestroy(e);
     if (copy_stream_) cudaStreamSynchronize(copy_stream_);
     if (leaf_ready_) cudaEventDestroy(leaf_ready_);
     if (copy_stream_) cudaStreamDestroy(copy_stream_);
@@ -565,11 +568,43 @@ void Builder::set_output_host(uint8_t* records, uint32_t* lut, uint64_t capacity
     }
 }
 
-void Builder::upload(const uint8_t* host_cloud, bool wait) {
+void Builder::upload(const uint8_t* host_cloud, bool wait, bool count) {
     TraceRange trace("upload");
     if (!host_cloud) throw Error("no point cloud set");
     tree_valid_ = false;
     reuse_tree_ = false;
+    counted_ = false;
+    constexpr uint32_t kChunks = 16;
+    constexpr uint64_t kChunkAlign = 1024;   // chunk starts: a multiple of the counting tile (16-byte aligned)
+    if (count && cfg_.has_bbox() && cfg_.n >= 4 * kChunks * kChunkAlign) {
+        const bool sparse = sparse_cloud();
+        while (chunk_ready_.size() < kChunks) {
+            cudaEvent_t e;
+            check_cuda(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
+            chunk_ready_.push_back(e);
+        }
+        stage_begin();
+        clear_for_count(sparse);
+        const CloudGrid g = cloud_grid();
+        const uint64_t per = ((cfg_.n + kChunks - 1) / kChunks + kChunkAlign - 1) / kChunkAlign * kChunkAlign;
+        uint32_t k = 0;
+        for (uint64_t first = 0; first < cfg_.n; first += per, ++k) {
+            const uint64_t cnt = std::min<uint64_t>(per, cfg_.n - first);
+            const size_t off = (size_t)first * cfg_.stride;
+            check_cuda(cudaMemcpyAsync(cloud_.as<uint8_t>() + off, host_cloud + off, (size_t)cnt * cfg_.stride,
+                                       cudaMemcpyHostToDevice, side_stream_),
+                       "cloud upload");
+            check_cuda(cudaEventRecord(chunk_ready_[k], side_stream_), "event");
+            check_cuda(cudaStreamWaitEvent(stream_, chunk_ready_[k], 0), "wait");
+            launch_count(cloud_.as<uint8_t>() + off, cnt, cfg_.stride, cfg_.cloud_type == 0, g, pyr_.as<uint32_t>(),
+                         sparse ? occ_.as<uint8_t>() : nullptr, err_.as<uint32_t>(), num_sms_, stream_);
+        }
+        check_cuda(cudaGetLastError(), "count launch");
+        stage_mark("upload_count");
+        counted_ = true;
+        if (wait) check_cuda(cudaStreamSynchronize(side_stream_), "upload sync");
+        return;
+    }
     if (!wait) {
         check_cuda(cudaMemcpyAsync(cloud_.p, host_cloud, (size_t)cfg_.n * cfg_.stride, cudaMemcpyHostToDevice, stream_),
                    "cloud upload");
@@ -600,6 +635,41 @@ void throw_device_errors(uint32_t e, const char* stage) {
     if (e & kErrTimeout) throw Error(std::string(stage) + ": a bulk copy did not complete in time");
 }
 
+CloudGrid Builder::cloud_grid() const {
+    const double cubic = cfg_.bb_max[0] - cfg_.bb_min[0];
+    CloudGrid g;
+    g.grid = cfg_.chunk_grid;
+    const double t0 = cubic / cfg_.chunk_grid;   // kernel_helpers.cuh:14
+    for (int a = 0; a < 3; ++a) {
+        g.ax[a] = make_axis(cfg_.bb_min[a], t0);
+        g.r[a] = (float)(1.0 / t0);
+        g.c[a] = (float)(-cfg_.bb_min[a] / t0);
+    }
+    g.keys = cell_keys_.p;
+    g.spread = spread_.as<uint32_t>();
+    return g;
+}
+
+// Sparse clouds (at most one point per 16 finest cells) flag the 64-cell
+// blocks of the finest level they touch (one byte per block): counting sets
+// the flags, the pyramid and the tag push skip unflagged blocks, and the build
+// ends by zeroing only the flagged blocks and the upper levels, so the next
+// build finds the pyramid zero.  Denser clouds clear the whole pyramid first.
+bool Builder::sparse_cloud() const {
+    return depth_ >= 2 && (uint64_t)cfg_.n * 16 <= level_off_[1];
+}
+
+// What counting accumulates into, cleared on the build stream.
+void Builder::clear_for_count(bool sparse) {
+    if (!sparse || !pyr_zero_) {
+        check_cuda(cudaMemsetAsync(pyr_.p, 0, level_off_[depth_ + 1] * 4, stream_), "memset");
+        if (sparse) check_cuda(cudaMemsetAsync(occ_.p, 0, level_off_[1] >> 6, stream_), "memset");
+    }
+    pyr_zero_ = false;
+    check_cuda(cudaMemsetAsync(err_.p, 0, 64, stream_), "memset");
+    check_cuda(cudaMemsetAsync(nonzero_.p, 0, (depth_ + 1) * 4, stream_), "memset");
+}
+
 void Builder::generate() {
     TraceRange trace(reuse_tree_ ? "generate (resident tree)" : "generate");
     host_filled_ = false;
@@ -624,44 +694,27 @@ void Builder::generate() {
     tree_valid_ = false;
     if (!cfg_.has_bbox()) throw Error("no bounding box: call ocpi_set_cloud_bb before ocpi_init_octree or ocpi_compute_cloud_bb after it");
     if (host_rec_ && host_cap_ < cfg_.n) throw Error("output host buffer holds fewer records than the cloud");
-    const double cubic = cfg_.bb_max[0] - cfg_.bb_min[0];
-    CloudGrid g;
-    g.grid = cfg_.chunk_grid;
-    const double t0 = cubic / cfg_.chunk_grid;   // kernel_helpers.cuh:14
-    for (int a = 0; a < 3; ++a) {
-        g.ax[a] = make_axis(cfg_.bb_min[a], t0);
-        g.r[a] = (float)(1.0 / t0);
-        g.c[a] = (float)(-cfg_.bb_min[a] / t0);
-    }
-    g.keys = cell_keys_.p;
-    g.spread = spread_.as<uint32_t>();
+    const CloudGrid g = cloud_grid();
     OutParams op;
     for (int a = 0; a < 3; ++a) op.ax[a] = make_out_axis(cfg_.bb_min[a], 1.0 / cfg_.scale[a]);   // octree_chunking.cu:109-111
     const bool f32 = cfg_.cloud_type == 0;
-
-    // Sparse clouds (at most one point per 16 finest cells) flag the 64-cell
-    // blocks of the finest level they touch (one byte per block): counting
-    // sets the flags, the pyramid and the tag push skip unflagged blocks, and
-    // the build ends by zeroing only the flagged blocks and the upper levels,
-    // so the next build finds the pyramid zero.  Denser clouds clear the
-    // whole pyramid first.
     const uint64_t cells0 = level_off_[1];
-    const bool sparse = depth_ >= 2 && (uint64_t)cfg_.n * 16 <= cells0;
+    const bool sparse = sparse_cloud();
     const uint64_t occ_blocks = cells0 >> 6;
     uint8_t* occ = sparse ? occ_.as<uint8_t>() : nullptr;
-    stage_begin();
-    if (!sparse || !pyr_zero_) {
-        check_cuda(cudaMemsetAsync(pyr_.p, 0, level_off_[depth_ + 1] * 4, stream_), "memset");
-        if (sparse) check_cuda(cudaMemsetAsync(occ_.p, 0, occ_blocks, stream_), "memset");
-    }
-    pyr_zero_ = false;
-    check_cuda(cudaMemsetAsync(err_.p, 0, 64, stream_), "memset");
-    check_cuda(cudaMemsetAsync(nonzero_.p, 0, (depth_ + 1) * 4, stream_), "memset");
-    stage_mark("clear");
     launches_ = 0;
-    launches_ += launch_count(cloud_.as<uint8_t>(), cfg_.n, cfg_.stride, f32, g, pyr_.as<uint32_t>(), occ,
-                              err_.as<uint32_t>(), num_sms_, stream_);
-    stage_mark("count");
+    if (counted_) {
+        // binned during the upload (overlapped with the copy); the stage
+        // events of that upload stay the first of this build
+        counted_ = false;
+    } else {
+        stage_begin();
+        clear_for_count(sparse);
+        stage_mark("clear");
+        launches_ += launch_count(cloud_.as<uint8_t>(), cfg_.n, cfg_.stride, f32, g, pyr_.as<uint32_t>(), occ,
+                                  err_.as<uint32_t>(), num_sms_, stream_);
+        stage_mark("count");
+    }
     launches_ += launch_pyramid(pyr_.as<uint32_t>(), level_off_.data(), depth_, nonzero_.as<uint32_t>(), occ, stream_);
     stage_mark("pyramid");
     launches_ += launch_enumerate(pyr_.as<uint32_t>(), loff_.as<uint64_t>(), depth_, cfg_.threshold, key_.as<uint32_t>(),

@@ -146,17 +146,21 @@ void throw_device_errors(uint32_t e, const char* stage);
 
 class Builder {
 public:
-    Builder(const BuildConfig& cfg, const uint8_t* host_cloud, int device);
+    // count = true: see upload().
+    Builder(const BuildConfig& cfg, const uint8_t* host_cloud, int device, bool count = false);
     ~Builder();
     Builder(const Builder&) = delete;
     Builder& operator=(const Builder&) = delete;
 
     // Uploads a new cloud of the same configuration (reuses allocations).
     // wait = false leaves the copy in flight on the build stream: the host
-    // cloud must then stay valid until generate() returns.
-    void upload(const uint8_t* host_cloud, bool wait = true);
+    // cloud must then stay valid until generate() returns.  count = true and
+    // a known bounding box: the copy goes in chunks on the side stream and
+    // each chunk is binned on the build stream as soon as it has landed, so
+    // counting hides under the copy and the next generate() skips it.
+    void upload(const uint8_t* host_cloud, bool wait = true, bool count = false);
     // A new configuration and cloud; buffers only grow (see size_for_config).
-    void reconfigure(const BuildConfig& cfg, const uint8_t* host_cloud, bool wait_upload = true);
+    void reconfigure(const BuildConfig& cfg, const uint8_t* host_cloud, bool wait_upload = true, bool count = false);
     // Resident state: after a successful generate(), the uploaded cloud, the
     // count pyramid, the node tree and the leaf records stay on the device.
     // If `cfg` differs from the last build only in its subsampling settings
@@ -199,6 +203,9 @@ private:
     void check_device_errors(const char* stage);
     void build_tree_host();
     void fill_cell_tables();
+    CloudGrid cloud_grid() const;
+    bool sparse_cloud() const;
+    void clear_for_count(bool sparse);
     void params_writable();
     void record_params();
     void size_for_config();
@@ -248,6 +255,8 @@ private:
     bool tree_valid_ = false;        // the device holds the tree and leaf records of cfg_ (last generate succeeded)
     bool bbox_from_device_ = false;  // cfg_'s box came from compute_bbox
     bool reuse_tree_ = false;        // the next generate() subsamples the resident tree
+    bool counted_ = false;           // upload() binned the cloud: the next generate() skips counting
+    std::vector<cudaEvent_t> chunk_ready_;   // chunks of an overlapped upload
     uint64_t sub_stage_cap_ = 0, sub_scratch_cap_ = 0, sub_rec_cap_ = 0;   // capacities that fit the last build
     uint32_t g_cap_ = 0, g_shift_ = 0;
     uint32_t launches_ = 0;

@@ -205,7 +205,9 @@ int ocpi_init_octree(void* session) {
         auto* s = to_session(session);
         oc::check_cuda(cudaSetDevice(s->device), "cudaSetDevice");
         if (s->builder && same_config(s->builder->config(), s->cfg)) {
-            s->builder->upload(s->host_cloud);   // same configuration: reuse device state
+            // same configuration: reuse device state; the upload goes in
+            // chunks and bins each chunk as it lands (when the box is known)
+            s->builder->upload(s->host_cloud, true, true);
             return;
         }
         if (s->builder) {
@@ -213,7 +215,7 @@ int ocpi_init_octree(void* session) {
             // failure part-way (an allocation) leaves buffers sized for neither
             // configuration, so the builder is dropped.
             try {
-                s->builder->reconfigure(s->cfg, s->host_cloud);
+                s->builder->reconfigure(s->cfg, s->host_cloud, true, true);
             } catch (...) {
                 s->builder.reset();
                 throw;
@@ -221,7 +223,7 @@ int ocpi_init_octree(void* session) {
             if (s->out_rec) s->builder->set_output_host(s->out_rec, s->out_lut, s->out_cap);
             return;
         }
-        s->builder = std::make_unique<oc::Builder>(s->cfg, s->host_cloud, s->device);
+        s->builder = std::make_unique<oc::Builder>(s->cfg, s->host_cloud, s->device, true);
         cudaDeviceGetAttribute(&s->builder_sms, cudaDevAttrMultiProcessorCount, s->device);
         if (s->out_rec) s->builder->set_output_host(s->out_rec, s->out_lut, s->out_cap);
     });
