@@ -659,11 +659,16 @@ bool Builder::sparse_cloud() const {
     return depth_ >= 2 && (uint64_t)cfg_.n * 16 <= level_off_[1];
 }
 
-// What counting accumulates into, cleared on the build stream.
+// What counting accumulates into, cleared on the build stream.  A sparse
+// build relies on the whole allocation being zero (a build on another grid
+// may have written beyond this grid's levels), so its full clear covers the
+// whole pyramid and flag allocations; a dense build clears its own levels.
 void Builder::clear_for_count(bool sparse) {
-    if (!sparse || !pyr_zero_) {
+    if (!sparse) {
         check_cuda(cudaMemsetAsync(pyr_.p, 0, level_off_[depth_ + 1] * 4, stream_), "memset");
-        if (sparse) check_cuda(cudaMemsetAsync(occ_.p, 0, level_off_[1] >> 6, stream_), "memset");
+    } else if (!pyr_zero_) {
+        check_cuda(cudaMemsetAsync(pyr_.p, 0, pyr_.bytes, stream_), "memset");
+        check_cuda(cudaMemsetAsync(occ_.p, 0, occ_.bytes, stream_), "memset");
     }
     pyr_zero_ = false;
     check_cuda(cudaMemsetAsync(err_.p, 0, 64, stream_), "memset");

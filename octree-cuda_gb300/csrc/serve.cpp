@@ -221,7 +221,8 @@ public:
 private:
     // The next job for lane l (mutex held): among the first 2 x lanes waiting
     // jobs, the oldest that names the lane's resident cloud; else the oldest
-    // waiting job that fits the budget.
+    // waiting job that fits the budget.  The window bounds how far a job can
+    // be overtaken.
     std::shared_ptr<Job> take(uint32_t l) {
         uint64_t others = 0;
         for (size_t k = 0; k < reserved_.size(); ++k)

@@ -253,3 +253,29 @@ def test_cancel_a_waiting_job():
             srv.cancel(t1)
     finally:
         srv.close()
+
+
+def test_session_sparse_builds_after_a_dense_build_on_other_grids():
+    """One session through a dense build on a 64 grid, a sparse build on a
+    32 grid, then a sparse build on the 64 grid (the first grid's finest
+    level must be clean again): every build equals the same build on a new
+    session."""
+    steps = [(make_case(0, 0, 100_000, seed=71), (64, 32)),   # dense: 100k points > 64^3 / 16
+             (make_case(1, 0, 1_500, seed=72), (32, 16)),      # sparse on the smaller grid
+             (make_case(2, 1, 10_000, seed=73), (64, 32))]     # sparse on the larger grid
+    s = octree_api.OctreeSession(0)
+    try:
+        for case, grids in steps:
+            want = alone(case, grids, 0)
+            s.set_cloud(case.cloud, n=case.n, stride=case.stride, cloud_type=case.cloud_type, scale=case.scale,
+                        bb_min=case.bb_min, bb_max=case.bb_max)
+            s.configure(chunk_grid=grids[0], sub_grid=grids[1], merge_threshold=2000, seed=99, **MODES[0])
+            s.init()
+            s.generate()
+            h = s.hierarchy()
+            assert h.tobytes() == want[0].tobytes(), grids
+            a_r, a_l = node_sorted(want[0], want[1], want[2])
+            b_r, b_l = node_sorted(h, s.records(), s.lut())
+            assert np.array_equal(a_l, b_l) and a_r.tobytes() == b_r.tobytes()
+    finally:
+        s.close()
