@@ -378,6 +378,11 @@ def run_batched(args):
         bad = [r.error.decode() for r in res if r.status != 0]
         if bad:
             raise RuntimeError("batched build failed: %s" % bad[0])
+        if not args.no_plain:
+            # every build of the batch has the shape of the same build run alone
+            for i, (r, (p, nn)) in enumerate(zip(res, shapes)):
+                if (r.pointsTotal, r.nodeCount) != (p, nn):
+                    raise RuntimeError("cloud %d: batched build differs from the plain build" % i)
         return dt, res
 
     if not args.no_plain:
@@ -486,6 +491,8 @@ def run_served(args):
             free.put(slot)
             if r.status != 0:
                 raise RuntimeError("request %d failed: %s" % (k, r.error.decode()))
+            if (r.pointsTotal, r.nodeCount) != shape[(int(req_cloud[k]), int(req_opt[k]))]:
+                raise RuntimeError("request %d: served build differs from the plain build" % k)
             lat[k] = done_at[k] - t_arr
 
         with concurrent.futures.ThreadPoolExecutor(max_workers=slots) as ex:
