@@ -279,3 +279,34 @@ def test_session_sparse_builds_after_a_dense_build_on_other_grids():
             assert np.array_equal(a_l, b_l) and a_r.tobytes() == b_r.tobytes()
     finally:
         s.close()
+
+
+def test_session_random_sequence_equals_fresh_builds():
+    """Twelve builds on one session, seeded at random: grids 32 to 128, point
+    amounts on both sides of the sparse-pyramid threshold (one point per 16
+    finest cells), all four subsampling modes.  Every build equals the same
+    build on a fresh session, whatever state the previous build left."""
+    rng = np.random.default_rng(2026)
+    s = octree_api.OctreeSession(0)
+    try:
+        for step in range(12):
+            g0 = int(rng.choice([32, 64, 128]))
+            g1 = int(rng.choice([16, 32])) if g0 > 32 else 16
+            cells = g0 ** 3
+            n = int(cells // 16 * rng.choice([0.3, 0.9, 1.5, 6.0]))
+            n = max(n, 2500)
+            m = int(rng.integers(0, len(MODES)))
+            case = make_case(int(rng.integers(0, 3)), int(rng.integers(0, 2)), n, seed=500 + step)
+            want = alone(case, (g0, g1), m)
+            s.set_cloud(case.cloud, n=case.n, stride=case.stride, cloud_type=case.cloud_type, scale=case.scale,
+                        bb_min=case.bb_min, bb_max=case.bb_max)
+            s.configure(chunk_grid=g0, sub_grid=g1, merge_threshold=2000, seed=99, **MODES[m])
+            s.init()
+            s.generate()
+            h = s.hierarchy()
+            assert h.tobytes() == want[0].tobytes(), (step, g0, n, m)
+            a_r, a_l = node_sorted(want[0], want[1], want[2])
+            b_r, b_l = node_sorted(h, s.records(), s.lut())
+            assert np.array_equal(a_l, b_l) and a_r.tobytes() == b_r.tobytes(), (step, g0, n, m)
+    finally:
+        s.close()
