@@ -513,6 +513,25 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
             if (threadIdx.x == 0) ns.cells = total;
         }
         sync_all();
+        // The brick map is final: cluster blocks other than rank 0 copy it from
+        // rank 0's shared memory into their own (unused until now), so that the
+        // cell list, pass B and emit read it locally instead of through
+        // distributed shared memory.
+        if constexpr (kCluster) {
+            if (crank != 0 && bm.key == sm_map.key) {
+                BrickMap local = bm;
+                local.mask = dyn;
+                local.key = reinterpret_cast<uint32_t*>(dyn + kBrickSlots);
+                local.base = local.key + kBrickSlots;
+                for (uint32_t i = threadIdx.x; i < bm.cap; i += blockDim.x) {
+                    local.mask[i] = bm.mask[i];
+                    local.key[i] = bm.key[i];
+                    local.base[i] = bm.base[i];
+                }
+                __syncthreads();
+                bm = local;
+            }
+        }
         // rank -> (brick slot, bit), for the per-cell emit.  A warp lists the
         // cells of its 32 consecutive slots (consecutive ranks) in rank order,
         // 32 ranks per coalesced store: each lane finds the slot holding its
