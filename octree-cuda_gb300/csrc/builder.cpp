@@ -226,6 +226,15 @@ void Builder::reconfigure(const BuildConfig& cfg, const uint8_t* host_cloud, boo
     reuse_tree_ = false;
     bbox_from_device_ = false;
     if (copy_stream_) check_cuda(cudaStreamSynchronize(copy_stream_), "output copies");
+    const bool adopt = prefetched_ && prefetched_ == host_cloud && prefetched_bytes_ == (uint64_t)cfg.n * cfg.stride;
+    prefetched_ = nullptr;
+    if (adopt) {
+        // the spare buffer becomes the cloud; the old cloud buffer is free for
+        // the next prefetch once the work queued on the build stream is done
+        std::swap(cloud_.p, spare_.p);
+        std::swap(cloud_.bytes, spare_.bytes);
+        check_cuda(cudaEventRecord(spare_free_, stream_), "event");
+    }
     cfg_ = cfg;
     host_rec_ = nullptr;
     host_lut_ = nullptr;
@@ -234,7 +243,36 @@ void Builder::reconfigure(const BuildConfig& cfg, const uint8_t* host_cloud, boo
     nodes_.clear();
     stats_ = Stats{};
     size_for_config();
-    upload(host_cloud, wait_upload, count);
+    if (!adopt) {
+        upload(host_cloud, wait_upload, count);
+        return;
+    }
+    counted_ = false;
+    check_cuda(cudaStreamWaitEvent(stream_, prefetch_done_, 0), "wait");
+    if (wait_upload) check_cuda(cudaStreamSynchronize(stream_), "upload sync");
+}
+
+void Builder::prefetch(const uint8_t* host_cloud, uint64_t bytes) {
+    prefetch_sync();
+    if (!prefetch_stream_) {
+        check_cuda(cudaStreamCreateWithFlags(&prefetch_stream_, cudaStreamNonBlocking), "stream");
+        check_cuda(cudaEventCreateWithFlags(&prefetch_done_, cudaEventDisableTiming), "event");
+        check_cuda(cudaEventCreateWithFlags(&spare_free_, cudaEventDisableTiming), "event");
+    }
+    if (spare_.bytes < bytes + 64) {
+        check_cuda(cudaStreamSynchronize(prefetch_stream_), "prefetch");
+        spare_.ensure(bytes + 64);   // same padding as the cloud buffer
+    }
+    check_cuda(cudaStreamWaitEvent(prefetch_stream_, spare_free_, 0), "wait");
+    check_cuda(cudaMemcpyAsync(spare_.p, host_cloud, bytes, cudaMemcpyHostToDevice, prefetch_stream_), "prefetch");
+    check_cuda(cudaEventRecord(prefetch_done_, prefetch_stream_), "event");
+    prefetched_ = host_cloud;
+    prefetched_bytes_ = bytes;
+}
+
+void Builder::prefetch_sync() {
+    if (prefetch_stream_) check_cuda(cudaStreamSynchronize(prefetch_stream_), "prefetch");
+    prefetched_ = nullptr;
 }
 
 // The staged parameter tables may be rewritten once their last upload is done.
@@ -393,6 +431,10 @@ bool Builder::reuse(const BuildConfig& c) {
 }
 
 Builder::~Builder() {
+    if (prefetch_stream_) cudaStreamSynchronize(prefetch_stream_);
+    if (prefetch_done_) cudaEventDestroy(prefetch_done_);
+    if (spare_free_) cudaEventDestroy(spare_free_);
+    if (prefetch_stream_) cudaStreamDestroy(prefetch_stream_);
     if (side_stream_) cudaStreamSynchronize(side_stream_);
     if (tree_ready_) cudaEventDestroy(tree_ready_);
     if (side_stream_) cudaStreamDestroy(side_stream_);
@@ -432,7 +474,7 @@ void Builder::collect_timings() {
 
 std::vector<std::pair<std::string, uint64_t>> Builder::device_allocations() const {
     return {
-        {"cloud", cloud_.bytes},
+        {"cloud", cloud_.bytes + spare_.bytes},
         {"count pyramid", pyr_.bytes + occ_.bytes},
         {"node table", key_.bytes + count_.bytes + level_.bytes + info_.bytes + child_first_.bytes +
                            data_idx_.bytes + fill_.bytes + level_start_.bytes + n_nodes_.bytes + loff_.bytes +
@@ -904,6 +946,7 @@ void Builder::subsample() {
     // order); internal index = position in the level-major order
     std::vector<uint32_t> level_first(depth_ + 2, 0), ii_of(n, 0xFFFFFFFFu);
     std::vector<uint32_t> order;
+    std::vector<uint32_t> balance(depth_ + 2, 1);   // see launch_subsample_level
     uint64_t max_level_bound = 0, max_node_bound = 0;
     for (uint32_t l = 1; l <= depth_; ++l) {
         auto list = internal_by_level_[l];
@@ -918,6 +961,7 @@ void Builder::subsample() {
             max_node_bound = std::max(max_node_bound, in_bound[vi]);
         }
         max_level_bound = std::max(max_level_bound, lb);
+        if (lb) balance[l] = (uint32_t)std::min<uint64_t>(64, (in_bound[list[0]] * num_sms_ + lb - 1) / lb);
     }
     level_first[depth_ + 1] = (uint32_t)order.size();
     const uint32_t n_internal = (uint32_t)order.size();
@@ -1110,7 +1154,7 @@ void Builder::subsample() {
             a.nodes = lvl;
             a.n_nodes = cnt;
             a.out_points = out_points_.as<uint32_t>() + first;
-            launches_ += launch_subsample_level(a, num_sms_, stream_);
+            launches_ += launch_subsample_level(a, num_sms_, balance[l], stream_);
             char mark[32];
             std::snprintf(mark, sizeof mark, "sub_l%u", l);
             stage_mark(mark);

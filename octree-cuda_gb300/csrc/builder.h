@@ -160,7 +160,18 @@ public:
     // counting hides under the copy and the next generate() skips it.
     void upload(const uint8_t* host_cloud, bool wait = true, bool count = false);
     // A new configuration and cloud; buffers only grow (see size_for_config).
+    // A cloud given to prefetch() before (same host pointer and size) is
+    // adopted from the spare buffer instead of being copied again.
     void reconfigure(const BuildConfig& cfg, const uint8_t* host_cloud, bool wait_upload = true, bool count = false);
+    // Starts copying the cloud of a later build (`bytes` from host_cloud)
+    // into a spare device buffer, on a stream of its own, so that the copy
+    // overlaps the build in progress.  The host cloud must stay valid until
+    // reconfigure() adopts it or prefetch_sync() returns.  Throws what an
+    // allocation throws; the spare buffer only grows.
+    void prefetch(const uint8_t* host_cloud, uint64_t bytes);
+    // Waits for a prefetch copy in flight and forgets it.
+    void prefetch_sync();
+    uint64_t spare_bytes() const { return spare_.bytes; }
     // Resident state: after a successful generate(), the uploaded cloud, the
     // count pyramid, the node tree and the leaf records stay on the device.
     // If `cfg` differs from the last build only in its subsampling settings
@@ -221,6 +232,9 @@ private:
     uint32_t node_cap_ = 0;
 
     DevBuf cloud_, pyr_, loff_, err_, nonzero_;
+    DevBuf spare_;                      // cloud of the next build, copied while this one runs
+    const uint8_t* prefetched_ = nullptr;   // host cloud in flight to spare_ (nullptr: none)
+    uint64_t prefetched_bytes_ = 0;
     DevBuf occ_;                        // sparse clouds: one flag byte per 64-cell block of the finest level
     bool pyr_zero_ = false;             // the pyramid and the flags are all zero (sparse clean-up ran)
     DevBuf key_, count_, level_, info_, child_first_, level_start_, n_nodes_;
@@ -242,6 +256,9 @@ private:
     cudaStream_t copy_stream_ = nullptr;
     cudaStream_t side_stream_ = nullptr;   // reads the node table while distribution runs
     cudaEvent_t tree_ready_ = nullptr;
+    cudaStream_t prefetch_stream_ = nullptr;
+    cudaEvent_t prefetch_done_ = nullptr;   // the spare buffer holds the prefetched cloud
+    cudaEvent_t spare_free_ = nullptr;      // the build stream's last use of the buffer that became spare
     cudaEvent_t leaf_ready_ = nullptr;
     DevBuf post_ii_, node_dst_, out_total_;   // post-order of internal nodes, their output positions, P_out
     HostBuf loff_host_, keys_host_, spread_host_;   // staged parameter tables (uploaded on the build stream)

@@ -26,6 +26,9 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <mutex>
+#include <set>
+#include <utility>
 
 #include "device_common.cuh"
 #include "kernels.h"
@@ -808,26 +811,46 @@ size_t subsample_smem_bytes() {
 namespace {
 
 // Blocks per node for a level of n_nodes nodes: the smallest power of two up
-// to 4 whose clusters cover the SMs (levels with at least one node per SM run
-// one block per node).  Measured per level on the 119.7M-point build: clusters
-// of 2 take a 100-node level from 0.54 to 0.34 ms; clusters of 8 are slower
-// than 4 on 10- to 40-node levels.
-uint32_t cluster_size(uint32_t n_nodes, int num_sms) {
+// to `cap` whose clusters cover the SMs (levels with at least one node per SM
+// run one block per node).  Measured per level on the 119.7M-point build:
+// clusters of 2 take a 100-node level from 0.54 to 0.34 ms; clusters of 8 are
+// slower than 4 on 10- to 40-node levels, so the cap is 4.  Distance-weighted
+// levels go up to 16 (a non-portable cluster size), and at least to the
+// level's balance_blocks: the neighbourhood walk per output cell makes a
+// level's largest nodes long.  On the 25.8M-point weighted build a cap of 16
+// takes the root from 3.34 to 1.46 ms and the 8-node level from 2.10 to
+// 1.13 ms (a cap of 8: 2.15 and 1.39 ms).
+// Allows clusters above the portable size of 8 for a kernel on the current
+// device (once per kernel and device; a refusal leaves smaller clusters).
+void allow_wide_clusters(const void* kernel) {
+    static std::mutex mu;
+    static std::set<std::pair<int, const void*>> done;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> g(mu);
+    if (!done.insert({dev, kernel}).second) return;
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)
+        cudaGetLastError();
+}
+
+uint32_t cluster_size(uint32_t n_nodes, int num_sms, uint32_t cap) {
     uint32_t c = 1;
-    while (c < 4 && (uint64_t)c * n_nodes < (uint64_t)num_sms) c <<= 1;
+    while (c < cap && (uint64_t)c * n_nodes < (uint64_t)num_sms) c <<= 1;
     return c;
 }
 
 template <bool kF32, int kColor, bool kRandom>
-void launch_one(const SubLevelArgs& a, int num_sms, size_t smem, cudaStream_t stream) {
-    const uint32_t cs = cluster_size(a.n_nodes, num_sms);
+void launch_one(const SubLevelArgs& a, int num_sms, uint32_t balance, size_t smem, cudaStream_t stream) {
+    uint32_t cs = cluster_size(a.n_nodes, num_sms, kColor == 3 ? 16u : 4u);
+    if (kColor == 3)
+        while (cs < 16 && cs < balance) cs <<= 1;
     if (cs > 1) {
         auto kern = k_subsample<kF32, kColor, kRandom, true>;
         allow_dynamic_smem(reinterpret_cast<const void*>(kern), smem);
+        if (cs > 8) allow_wide_clusters(reinterpret_cast<const void*>(kern));
         cudaLaunchConfig_t cfg = {};
         cudaLaunchAttribute attr[1];
         attr[0].id = cudaLaunchAttributeClusterDimension;
-        attr[0].val.clusterDim.x = cs;
         attr[0].val.clusterDim.y = 1;
         attr[0].val.clusterDim.z = 1;
         cfg.blockDim = dim3(kSubThreads);
@@ -835,14 +858,19 @@ void launch_one(const SubLevelArgs& a, int num_sms, size_t smem, cudaStream_t st
         cfg.stream = stream;
         cfg.attrs = attr;
         cfg.numAttrs = 1;
-        cfg.gridDim = dim3(cs);
-        int max_clusters = 0;
-        if (cudaOccupancyMaxActiveClusters(&max_clusters, kern, &cfg) == cudaSuccess && max_clusters > 0) {
-            const uint32_t clusters = std::min<uint32_t>(a.n_nodes, (uint32_t)max_clusters);
-            cfg.gridDim = dim3(clusters * cs);
-            if (cudaLaunchKernelEx(&cfg, kern, a) == cudaSuccess) return;
+        // the largest cluster size up to cs of which one cluster fits
+        for (uint32_t c = cs; c > 1; c >>= 1) {
+            attr[0].val.clusterDim.x = c;
+            cfg.gridDim = dim3(c);
+            int max_clusters = 0;
+            if (cudaOccupancyMaxActiveClusters(&max_clusters, kern, &cfg) == cudaSuccess && max_clusters > 0) {
+                const uint32_t clusters = std::min<uint32_t>(a.n_nodes, (uint32_t)max_clusters);
+                cfg.gridDim = dim3(clusters * c);
+                if (cudaLaunchKernelEx(&cfg, kern, a) == cudaSuccess) return;
+            }
+            cudaGetLastError();
         }
-        cudaGetLastError();   // no cluster of this size fits: one block per node
+        // no cluster fits: one block per node
     }
     auto kern = k_subsample<kF32, kColor, kRandom, false>;
     allow_dynamic_smem(reinterpret_cast<const void*>(kern), smem);
@@ -851,31 +879,31 @@ void launch_one(const SubLevelArgs& a, int num_sms, size_t smem, cudaStream_t st
 }
 
 template <bool kF32>
-void launch_mode(const SubLevelArgs& a, int num_sms, size_t smem, cudaStream_t stream) {
+void launch_mode(const SubLevelArgs& a, int num_sms, uint32_t balance, size_t smem, cudaStream_t stream) {
     const bool intra = (a.mode & kModeIntra) != 0;
     const bool inter = !intra && (a.mode & kModeInter) != 0;
     const bool weighted = inter && (a.mode & kModeWeight) != 0;
     const int color = intra ? 1 : (weighted ? 3 : (inter ? 2 : 0));
     const bool random = (a.mode & kModeRandom) != 0;
     switch (color * 2 + (random ? 1 : 0)) {
-    case 0: launch_one<kF32, 0, false>(a, num_sms, smem, stream); break;
-    case 1: launch_one<kF32, 0, true>(a, num_sms, smem, stream); break;
-    case 2: launch_one<kF32, 1, false>(a, num_sms, smem, stream); break;
-    case 3: launch_one<kF32, 1, true>(a, num_sms, smem, stream); break;
-    case 4: launch_one<kF32, 2, false>(a, num_sms, smem, stream); break;
-    case 5: launch_one<kF32, 2, true>(a, num_sms, smem, stream); break;
-    case 6: launch_one<kF32, 3, false>(a, num_sms, smem, stream); break;
-    default: launch_one<kF32, 3, true>(a, num_sms, smem, stream); break;
+    case 0: launch_one<kF32, 0, false>(a, num_sms, balance, smem, stream); break;
+    case 1: launch_one<kF32, 0, true>(a, num_sms, balance, smem, stream); break;
+    case 2: launch_one<kF32, 1, false>(a, num_sms, balance, smem, stream); break;
+    case 3: launch_one<kF32, 1, true>(a, num_sms, balance, smem, stream); break;
+    case 4: launch_one<kF32, 2, false>(a, num_sms, balance, smem, stream); break;
+    case 5: launch_one<kF32, 2, true>(a, num_sms, balance, smem, stream); break;
+    case 6: launch_one<kF32, 3, false>(a, num_sms, balance, smem, stream); break;
+    default: launch_one<kF32, 3, true>(a, num_sms, balance, smem, stream); break;
     }
 }
 
 }   // namespace
 
-int launch_subsample_level(const SubLevelArgs& a, int num_sms, cudaStream_t stream) {
+int launch_subsample_level(const SubLevelArgs& a, int num_sms, uint32_t balance_blocks, cudaStream_t stream) {
     if (!a.n_nodes) return 0;
     size_t smem = subsample_smem_bytes();
-    if (a.float_input) launch_mode<true>(a, num_sms, smem, stream);
-    else launch_mode<false>(a, num_sms, smem, stream);
+    if (a.float_input) launch_mode<true>(a, num_sms, balance_blocks, smem, stream);
+    else launch_mode<false>(a, num_sms, balance_blocks, smem, stream);
     return 1;
 }
 

@@ -179,7 +179,11 @@ int launch_prepare_level(SubNode* nodes, uint32_t n_nodes, const uint32_t* out_p
 
 size_t subsample_smem_bytes();
 uint32_t subsample_block_size();
-int launch_subsample_level(const SubLevelArgs& a, int num_sms, cudaStream_t stream);
+// balance_blocks: the blocks the level's largest node needs for its share
+// of the work to equal one SM's share of the whole level (largest candidate
+// bound x SMs / sum of the bounds); distance-weighted levels size their
+// clusters by it.
+int launch_subsample_level(const SubLevelArgs& a, int num_sms, uint32_t balance_blocks, cudaStream_t stream);
 
 // Raises a kernel's dynamic shared memory limit on the current device to at
 // least `bytes` and never lowers it, so that builders launching the same

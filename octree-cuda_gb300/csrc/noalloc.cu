@@ -201,7 +201,7 @@ extern "C" int ocpi_subsample_node_noalloc(const uint8_t* cloud, uint8_t cloudTy
         a.global_base = reinterpret_cast<uint32_t*>(base + kOffGBase);
         a.global_cap = (uint32_t)cap;
         a.global_shift = shift;
-        launch_subsample_level(a, 1, st);
+        launch_subsample_level(a, 1, 1, st);
         check_cuda(cudaGetLastError(), "ocpi_subsample_node_noalloc launch");
         return SUCCESS;
     } catch (const std::exception& e) {

@@ -8,6 +8,13 @@
 // While one lane waits on its host steps (tree read-back, level
 // bookkeeping, the final read-back), the others keep the GPU busy.
 //
+// Prefetch: under a backlog (every lane busy, at least as many jobs waiting
+// as lanes) a lane that starts a job also takes the job it will run next
+// and copies that job's cloud into a spare device buffer on a stream of its
+// own, so that the host-to-device copy overlaps the build in progress
+// instead of preceding the next one.  The spare buffer counts in the lane's
+// reservation.
+//
 // Admission: a job's device memory is bounded by estimate_device_bytes.  A
 // lane reserves the bound of the envelope of the jobs its builder has run
 // (buffers only grow, each to the largest size any of those jobs needed); a
@@ -63,6 +70,7 @@ struct Job {
     uint64_t bound = 0;   // device bytes (estimate_device_bytes)
     Clock::time_point submitted, started, finished;
     bool done = false;
+    bool cancel_requested = false;   // cancelled while held by a lane
     OcpiJobResult result{};
     std::vector<uint8_t> hierarchy;
 };
@@ -113,6 +121,9 @@ public:
         resident_cfg_.assign(lanes, BuildConfig{});
         busy_.assign(lanes, false);
         releasing_.assign(lanes, false);
+        held_.assign(lanes, nullptr);
+        held_copy_.assign(lanes, false);
+        spare_.assign(lanes, 0);
         for (uint32_t l = 0; l < lanes; ++l) workers_.emplace_back([this, l] { run_lane(l); });
     }
 
@@ -180,7 +191,9 @@ public:
     }
 
     // A waiting job leaves the queue and completes as failed ("cancelled");
-    // a running or completed job cannot be cancelled.
+    // a job held by a lane completes so once that lane has finished its
+    // current job and its copy of the held job's cloud; a running or
+    // completed job cannot be cancelled.
     void cancel(uint64_t ticket) {
         {
             std::lock_guard<std::mutex> g(mu_);
@@ -189,7 +202,11 @@ public:
             auto job = it->second;
             if (job->done) throw Error("the job has already completed");
             auto q = std::find(queue_.begin(), queue_.end(), job);
-            if (q == queue_.end()) throw Error("the job is running");
+            if (q == queue_.end()) {
+                if (std::find(held_.begin(), held_.end(), job) == held_.end()) throw Error("the job is running");
+                job->cancel_requested = true;
+                return;
+            }
             queue_.erase(q);
             job->finished = Clock::now();
             job->started = job->finished;
@@ -232,7 +249,7 @@ private:
             for (auto it = queue_.begin(); it != queue_.end() && seen < 2 * reserved_.size(); ++it, ++seen) {
                 if ((*it)->spec.cloudId != resident_[l] || !same_chunking(resident_cfg_[l], (*it)->cfg)) continue;
                 const MemoryTerms env = envelope(env_[l], (*it)->terms);
-                const uint64_t mine = device_bytes(env);
+                const uint64_t mine = device_bytes(env) + spare_[l];
                 if (others + mine > budget_) continue;
                 auto job = *it;
                 queue_.erase(it);
@@ -243,7 +260,7 @@ private:
         }
         for (auto it = queue_.begin(); it != queue_.end(); ++it) {
             const MemoryTerms env = envelope(env_[l], (*it)->terms);
-            const uint64_t mine = device_bytes(env);
+            const uint64_t mine = device_bytes(env) + spare_[l];
             if (others + mine <= budget_) {
                 auto job = *it;
                 queue_.erase(it);
@@ -253,6 +270,58 @@ private:
             }
         }
         return nullptr;
+    }
+
+    // The job lane l starts after `cur` (mutex held), taken while cur runs so
+    // that its cloud is copied during cur's build.  Only under a backlog:
+    // every lane busy and at least as many jobs waiting as there are lanes,
+    // so that no waiting job is held back from a lane about to go idle.
+    // Among the first 2 x lanes waiting jobs, one naming cur's cloud (its
+    // state stays resident, nothing to copy) comes first; else the oldest job
+    // that fits the budget with the lane's spare cloud buffer grown for it.
+    // *copy: the job's cloud is to be prefetched.
+    std::shared_ptr<Job> hold(uint32_t l, const Job& cur, bool* copy) {
+        *copy = false;
+        if (queue_.size() < busy_.size()) return nullptr;
+        for (size_t k = 0; k < busy_.size(); ++k)
+            if (!busy_[k]) return nullptr;
+        uint64_t others = 0;
+        for (size_t k = 0; k < reserved_.size(); ++k)
+            if (k != l) others += reserved_[k];
+        auto admit = [&](std::deque<std::shared_ptr<Job>>::iterator it, uint64_t spare) -> std::shared_ptr<Job> {
+            const MemoryTerms env = envelope(env_[l], (*it)->terms);
+            const uint64_t mine = device_bytes(env) + spare;
+            if (others + mine > budget_) return nullptr;
+            auto job = *it;
+            queue_.erase(it);
+            env_[l] = env;
+            reserved_[l] = mine;
+            spare_[l] = spare;
+            return job;
+        };
+        if (cur.spec.cloudId) {
+            size_t seen = 0;
+            for (auto it = queue_.begin(); it != queue_.end() && seen < 2 * reserved_.size(); ++it, ++seen)
+                if ((*it)->spec.cloudId == cur.spec.cloudId && same_chunking(cur.cfg, (*it)->cfg))
+                    if (auto job = admit(it, spare_[l])) return job;
+        }
+        for (auto it = queue_.begin(); it != queue_.end(); ++it) {
+            const uint64_t need = std::max<uint64_t>(spare_[l], (uint64_t)(*it)->cfg.n * (*it)->cfg.stride + 64);
+            if (auto job = admit(it, need)) {
+                *copy = true;
+                return job;
+            }
+        }
+        return nullptr;
+    }
+
+    // A held job goes back to the front of the queue (mutex held): its lane
+    // lost its builder, and with it the prefetched cloud and the reservation.
+    void unhold(uint32_t l) {
+        if (!held_[l]) return;
+        queue_.push_front(held_[l]);
+        held_[l] = nullptr;
+        held_copy_[l] = false;
     }
 
     // True when idle lane l should give its memory back to a waiting job
@@ -311,6 +380,8 @@ private:
             reserved_[l] = 0;
             env_[l] = MemoryTerms{};
             resident_[l] = 0;
+            spare_[l] = 0;
+            unhold(l);
         }
         cv_done_.notify_all();
         cv_work_.notify_all();
@@ -320,22 +391,60 @@ private:
         std::unique_ptr<Builder> builder;
         for (;;) {
             std::shared_ptr<Job> job;
-            bool shrink = false;
+            bool shrink = false, prefetched = false, drop = false;
             {
                 std::unique_lock<std::mutex> g(mu_);
-                cv_work_.wait(g, [&] {
-                    if (stop_) return true;
-                    job = take(l);
-                    if (job) return true;
-                    shrink = blocked_by(l);   // idle and holding memory a waiting job needs
-                    return shrink;
-                });
-                if (!job && !shrink) return;   // stopping
-                if (shrink) releasing_[l] = true;
-                if (job) {
+                if (held_[l]) {
+                    job = held_[l];
+                    prefetched = held_copy_[l];
+                    held_[l] = nullptr;
+                    held_copy_[l] = false;
+                    drop = stop_ || job->cancel_requested;
+                } else {
+                    cv_work_.wait(g, [&] {
+                        if (stop_) return true;
+                        job = take(l);
+                        if (job) return true;
+                        shrink = blocked_by(l);   // idle and holding memory a waiting job needs
+                        return shrink;
+                    });
+                    if (!job && !shrink) return;   // stopping
+                    if (shrink) releasing_[l] = true;
+                }
+                if (job && !drop) {
                     busy_[l] = true;
                     job->started = Clock::now();
                 }
+            }
+            if (drop) {
+                // a held job cancelled, or the executor stopping: its cloud
+                // copy ends before the job completes and its owner may free it
+                try {
+                    if (builder) builder->prefetch_sync();
+                } catch (const std::exception&) {
+                    builder.reset();
+                    cudaGetLastError();
+                }
+                {
+                    std::lock_guard<std::mutex> g(mu_);
+                    job->finished = job->started = Clock::now();
+                    OcpiJobResult r{};
+                    r.status = -1;
+                    std::snprintf(r.error, sizeof r.error, "%s",
+                                  job->cancel_requested ? "cancelled" : "server destroyed before the job started");
+                    r.queuedMs = r.totalMs = ms_between(job->submitted, job->finished);
+                    job->result = r;
+                    job->done = true;
+                    if (!builder) {
+                        reserved_[l] = 0;
+                        env_[l] = MemoryTerms{};
+                        resident_[l] = 0;
+                        spare_[l] = 0;
+                    }
+                }
+                cv_done_.notify_all();
+                cv_work_.notify_all();
+                continue;
             }
             if (!job) {
                 builder.reset();   // frees this lane's buffers
@@ -344,6 +453,7 @@ private:
                     reserved_[l] = 0;
                     env_[l] = MemoryTerms{};
                     resident_[l] = 0;
+                    spare_[l] = 0;
                     releasing_[l] = false;
                 }
                 cv_work_.notify_all();
@@ -358,6 +468,7 @@ private:
             std::vector<uint8_t> hier;
             try {
                 TraceRange trace("job");
+                if (builder && !prefetched) builder->prefetch_sync();   // a copy made for no job of this lane
                 const OcpiJob& s = job->spec;
                 BuildConfig cfg = job->cfg;
                 const bool device_bb = !cfg.has_bbox();
@@ -377,6 +488,29 @@ private:
                     }
                 }
                 r.reused = reuse ? 1u : 0u;
+                {
+                    // under a backlog, hold the next job and copy its cloud
+                    // while this build runs
+                    bool copy = false;
+                    std::shared_ptr<Job> next;
+                    {
+                        std::lock_guard<std::mutex> g(mu_);
+                        next = hold(l, *job, &copy);
+                        if (next) {
+                            held_[l] = next;
+                            held_copy_[l] = copy;
+                        }
+                    }
+                    if (next && copy) {
+                        try {
+                            builder->prefetch(next->spec.cloud, (uint64_t)next->cfg.n * next->cfg.stride);
+                        } catch (const std::exception&) {
+                            cudaGetLastError();   // no spare buffer: the held job uploads when it starts
+                            std::lock_guard<std::mutex> g(mu_);
+                            held_copy_[l] = false;
+                        }
+                    }
+                }
                 if (s.outRecords) builder->set_output_host(s.outRecords, s.outLut, s.outCapacity);
                 builder->generate();
                 hier = builder->hierarchy();
@@ -417,6 +551,8 @@ private:
                     reserved_[l] = 0;
                     env_[l] = MemoryTerms{};
                     resident_[l] = 0;
+                    spare_[l] = 0;
+                    unhold(l);
                 }
             }
             cv_done_.notify_all();
@@ -436,6 +572,9 @@ private:
     std::vector<uint64_t> resident_;   // cloud id whose tree each lane's builder holds (0: none)
     std::vector<BuildConfig> resident_cfg_;   // the configuration that tree was built with
     std::vector<bool> busy_, releasing_;
+    std::vector<std::shared_ptr<Job>> held_;   // the job each lane starts next, out of the queue
+    std::vector<bool> held_copy_;              // its cloud is being copied to the lane's spare buffer
+    std::vector<uint64_t> spare_;              // device bytes of each lane's spare cloud buffer
     std::vector<std::thread> workers_;
     uint64_t next_ticket_ = 0;
     uint64_t lane_restarts_ = 0;

@@ -255,6 +255,30 @@ def test_cancel_a_waiting_job():
         srv.close()
 
 
+def test_backlog_on_one_lane_with_held_jobs():
+    """One lane and a backlog: while a build runs, the lane holds the next job
+    and copies its cloud ahead.  Jobs share clouds in turn (each job's cloud
+    differs from the one before it), one waiting job is cancelled whether it
+    is held or still queued, and every other result equals its build alone."""
+    cases = [make_case(k % 3, k % 2, n, seed=80 + k) for k, n in enumerate((900_000, 300_000, 150_000, 250_000))]
+    order = [0, 1, 2, 3, 1, 0, 2, 1]
+    want = {k: alone(cases[k], (128, 64), 2 * (k % 2)) for k in set(order)}
+    srv = octree_api.Server(lanes=1, memory_budget=64 << 30)
+    try:
+        bufs = [buffers(want[k]) for k in order]
+        tickets = [srv.submit(job_for(cases[k], (128, 64), 2 * (k % 2), *b)) for k, b in zip(order, bufs)]
+        srv.cancel(tickets[2])
+        for i, (k, t) in enumerate(zip(order, tickets)):
+            r = srv.wait(t)
+            if i == 2:
+                assert r.status == -1 and r.error == b"cancelled"
+            else:
+                check_same(want[k], r, *bufs[i])
+            srv.release(t)
+    finally:
+        srv.close()
+
+
 def test_session_sparse_builds_after_a_dense_build_on_other_grids():
     """One session through a dense build on a 64 grid, a sparse build on a
     32 grid, then a sparse build on the 64 grid (the first grid's finest
