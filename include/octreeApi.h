@@ -208,7 +208,9 @@ OCPI_EXPORT int ocpi_server_wait(void* server, uint64_t ticket, OcpiJobResult* r
 OCPI_EXPORT int ocpi_server_get_hierarchy(void* server, uint64_t ticket, uint8_t* out);
 /* forgets a completed job (waits for it first) */
 OCPI_EXPORT int ocpi_server_release(void* server, uint64_t ticket);
-/* a waiting job completes at once as failed ("cancelled"); -1 if it is running or done */
+/* a waiting job completes as failed ("cancelled"): at once when queued, and
+   after its lane's current job when a lane already holds it; -1 if it is
+   running or done */
 OCPI_EXPORT int ocpi_server_cancel(void* server, uint64_t ticket);
 /* how many times a lane restarted after losing its worker */
 OCPI_EXPORT int ocpi_server_lane_restarts(void* server, uint64_t* restarts);
