@@ -317,11 +317,24 @@ private:
 
     // A held job goes back to the front of the queue (mutex held): its lane
     // lost its builder, and with it the prefetched cloud and the reservation.
+    // The builder is gone, so no copy of the job's cloud is in flight; a job
+    // cancelled while held completes as cancelled (the caller notifies).
     void unhold(uint32_t l) {
         if (!held_[l]) return;
-        queue_.push_front(held_[l]);
+        auto job = held_[l];
         held_[l] = nullptr;
         held_copy_[l] = false;
+        if (!job->cancel_requested) {
+            queue_.push_front(job);
+            return;
+        }
+        job->finished = job->started = Clock::now();
+        OcpiJobResult r{};
+        r.status = -1;
+        std::snprintf(r.error, sizeof r.error, "cancelled");
+        r.queuedMs = r.totalMs = ms_between(job->submitted, job->finished);
+        job->result = r;
+        job->done = true;
     }
 
     // True when idle lane l should give its memory back to a waiting job
