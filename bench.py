@@ -564,7 +564,7 @@ def main():
     ap.add_argument("--form", default="plain", choices=["plain", "batched", "served"],
                     help="plain: the 120M-point build; batched / served: many independent builds at once")
     ap.add_argument("--lanes", type=int, default=None,
-                    help="concurrent builds of the batched (default 4) and served (default 8) forms")
+                    help="concurrent builds of the batched and served forms (default 4)")
     ap.add_argument("--budget-gb", type=int, default=150, help="device memory budget of the batched / served forms")
     ap.add_argument("--clouds", type=int, default=256, help="clouds of the batched form")
     ap.add_argument("--requests", type=int, default=2000, help="requests of the served form")
@@ -586,7 +586,7 @@ def main():
         args.lanes = args.lanes or 4
         return run_batched(args)
     if args.form == "served":
-        args.lanes = args.lanes or 8
+        args.lanes = args.lanes or 4
         return run_served(args)
 
     import octree_api
