@@ -327,14 +327,23 @@ struct WeightedSum {
 // the shared memory of cluster rank 0 and the other blocks reach them through
 // distributed shared memory; candidates and cells are split over all blocks
 // of the cluster, and cluster barriers separate the phases.
-template <bool kF32, int kColor, bool kRandom, bool kCluster>
-__global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
+// The level arguments of the build a node belongs to: the launch's own, or
+// (a wave over several builds) the node's entry of the table.
+template <bool kWave>
+__device__ __forceinline__ const SubLevelArgs& node_args(const SubLevelArgs& a0, const WaveNodes& wn, uint32_t ni) {
+    if constexpr (kWave) return wn.clouds[wn.cloud_of[ni]];
+    else return a0;
+}
+
+template <bool kF32, int kColor, bool kRandom, bool kCluster, bool kWave>
+__global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a0, WaveNodes wn) {
     namespace cg = cooperative_groups;
     extern __shared__ uint64_t dyn[];
     __shared__ NodeShared ns;
     __shared__ uint32_t warp_sums[32];
     __shared__ uint32_t s_bricks, s_overflow;
     __shared__ uint32_t s_run_total, s_run_off;   // weighted: this block's run of cells in the CSR scan
+    __shared__ uint32_t s_skip_node;               // wave: the node's build overflowed a buffer
     const uint32_t csize = kCluster ? cg::this_cluster().num_blocks() : 1u;
     const uint32_t crank = kCluster ? cg::this_cluster().block_rank() : 0u;
     const uint32_t tid0 = crank * blockDim.x + threadIdx.x;   // this thread's index within the node's workers
@@ -360,16 +369,16 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
     sm_map.base = sm_map.key + kBrickSlots;
     sm_map.cap = kBrickSlots;
     sm_map.shift = kBrickShift;
-    sm_map.grid = a.grid;
-    sm_map.bs = (a.grid + 3) >> 2;
+    sm_map.grid = a0.grid;
+    sm_map.bs = (a0.grid + 3) >> 2;
     // per-block (per-cluster) brick table in global memory for nodes that outgrow shared memory
     const uint64_t owner_block = blockIdx.x / csize;
     BrickMap gl_map = sm_map;
-    gl_map.cap = a.global_cap;
-    gl_map.shift = a.global_shift;
-    gl_map.mask = a.global_mask + owner_block * a.global_cap;
-    gl_map.key = a.global_key + owner_block * a.global_cap;
-    gl_map.base = a.global_base + owner_block * a.global_cap;
+    gl_map.cap = a0.global_cap;
+    gl_map.shift = a0.global_shift;
+    gl_map.mask = a0.global_mask + owner_block * a0.global_cap;
+    gl_map.key = a0.global_key + owner_block * a0.global_cap;
+    gl_map.base = a0.global_base + owner_block * a0.global_cap;
 
     constexpr bool intra = kColor == 1;
     constexpr bool inter = kColor >= 2;
@@ -377,15 +386,33 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
     constexpr bool random = kRandom;
     constexpr bool averaged = intra || inter;
 
+    uint32_t* p_skip_node = owner(&s_skip_node);
     for (;;) {
-        if (crank == 0 && threadIdx.x == 0) ns.node = atomicAdd(a.work_counter, 1u);
+        if (crank == 0 && threadIdx.x == 0) {
+            const uint32_t k = atomicAdd(a0.work_counter, 1u);
+            ns.node = k;
+            // a wave skips the nodes of a build whose level did not fit its
+            // buffers (that build's pass is repeated on its own)
+            if constexpr (kWave) s_skip_node = k < a0.n_nodes && (*node_args<kWave>(a0, wn, k).err & kErrCapacity);
+        }
         sync_all();
         const uint32_t ni = ns0->node;
-        if (ni >= a.n_nodes) {
+        if (ni >= a0.n_nodes) {
             sync_all();   // rank 0's shared memory stays valid until every block has read it
             break;
         }
-        const SubNode& nd = a.nodes[ni];
+        const SubLevelArgs& a = node_args<kWave>(a0, wn, ni);
+        const uint32_t li = kWave ? wn.local[ni] : ni;   // the node's index in its build's level
+        if constexpr (kWave) {
+            const bool skip = *(volatile uint32_t*)p_skip_node != 0;
+            sync_all();
+            if (skip) continue;
+            sm_map.grid = a.grid;
+            sm_map.bs = (a.grid + 3) >> 2;
+            gl_map.grid = sm_map.grid;
+            gl_map.bs = sm_map.bs;
+        }
+        const SubNode& nd = kWave ? *wn.node[ni] : a.nodes[ni];
         if (threadIdx.x == 0) {
             ns.nchild = nd.nchild;
             ns.kind = nd.child_kind;
@@ -496,7 +523,7 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
         const bool failed = *(volatile uint32_t*)p_overflow != 0;
         sync_all();
         if (failed) {
-            if (crank == 0 && threadIdx.x == 0) a.out_points[ni] = 0;
+            if (crank == 0 && threadIdx.x == 0) a.out_points[li] = 0;
             continue;
         }
 
@@ -741,7 +768,7 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a) {
             }
             store_run(a.out_rec + (oo + r0) * 18, 0, min(32u, cells - r0), nw, stage);
         }
-        if (crank == 0 && threadIdx.x == 0) a.out_points[ni] = cells;
+        if (crank == 0 && threadIdx.x == 0) a.out_points[li] = cells;
         sync_all();
     }
 }
@@ -839,13 +866,14 @@ uint32_t cluster_size(uint32_t n_nodes, int num_sms, uint32_t cap) {
     return c;
 }
 
-template <bool kF32, int kColor, bool kRandom>
-void launch_one(const SubLevelArgs& a, int num_sms, uint32_t balance, size_t smem, cudaStream_t stream) {
+template <bool kF32, int kColor, bool kRandom, bool kWave>
+void launch_one(const SubLevelArgs& a, const WaveNodes& wn, int num_sms, uint32_t balance, size_t smem,
+                cudaStream_t stream) {
     uint32_t cs = cluster_size(a.n_nodes, num_sms, kColor == 3 ? 16u : 4u);
     if (kColor == 3)
         while (cs < 16 && cs < balance) cs <<= 1;
     if (cs > 1) {
-        auto kern = k_subsample<kF32, kColor, kRandom, true>;
+        auto kern = k_subsample<kF32, kColor, kRandom, true, kWave>;
         allow_dynamic_smem(reinterpret_cast<const void*>(kern), smem);
         if (cs > 8) allow_wide_clusters(reinterpret_cast<const void*>(kern));
         cudaLaunchConfig_t cfg = {};
@@ -866,34 +894,35 @@ void launch_one(const SubLevelArgs& a, int num_sms, uint32_t balance, size_t sme
             if (cudaOccupancyMaxActiveClusters(&max_clusters, kern, &cfg) == cudaSuccess && max_clusters > 0) {
                 const uint32_t clusters = std::min<uint32_t>(a.n_nodes, (uint32_t)max_clusters);
                 cfg.gridDim = dim3(clusters * c);
-                if (cudaLaunchKernelEx(&cfg, kern, a) == cudaSuccess) return;
+                if (cudaLaunchKernelEx(&cfg, kern, a, wn) == cudaSuccess) return;
             }
             cudaGetLastError();
         }
         // no cluster fits: one block per node
     }
-    auto kern = k_subsample<kF32, kColor, kRandom, false>;
+    auto kern = k_subsample<kF32, kColor, kRandom, false, kWave>;
     allow_dynamic_smem(reinterpret_cast<const void*>(kern), smem);
     const int grid = (int)std::min<uint32_t>(a.n_nodes, (uint32_t)num_sms);
-    kern<<<grid, kSubThreads, smem, stream>>>(a);
+    kern<<<grid, kSubThreads, smem, stream>>>(a, wn);
 }
 
-template <bool kF32>
-void launch_mode(const SubLevelArgs& a, int num_sms, uint32_t balance, size_t smem, cudaStream_t stream) {
+template <bool kF32, bool kWave>
+void launch_mode(const SubLevelArgs& a, const WaveNodes& wn, int num_sms, uint32_t balance, size_t smem,
+                 cudaStream_t stream) {
     const bool intra = (a.mode & kModeIntra) != 0;
     const bool inter = !intra && (a.mode & kModeInter) != 0;
     const bool weighted = inter && (a.mode & kModeWeight) != 0;
     const int color = intra ? 1 : (weighted ? 3 : (inter ? 2 : 0));
     const bool random = (a.mode & kModeRandom) != 0;
     switch (color * 2 + (random ? 1 : 0)) {
-    case 0: launch_one<kF32, 0, false>(a, num_sms, balance, smem, stream); break;
-    case 1: launch_one<kF32, 0, true>(a, num_sms, balance, smem, stream); break;
-    case 2: launch_one<kF32, 1, false>(a, num_sms, balance, smem, stream); break;
-    case 3: launch_one<kF32, 1, true>(a, num_sms, balance, smem, stream); break;
-    case 4: launch_one<kF32, 2, false>(a, num_sms, balance, smem, stream); break;
-    case 5: launch_one<kF32, 2, true>(a, num_sms, balance, smem, stream); break;
-    case 6: launch_one<kF32, 3, false>(a, num_sms, balance, smem, stream); break;
-    default: launch_one<kF32, 3, true>(a, num_sms, balance, smem, stream); break;
+    case 0: launch_one<kF32, 0, false, kWave>(a, wn, num_sms, balance, smem, stream); break;
+    case 1: launch_one<kF32, 0, true, kWave>(a, wn, num_sms, balance, smem, stream); break;
+    case 2: launch_one<kF32, 1, false, kWave>(a, wn, num_sms, balance, smem, stream); break;
+    case 3: launch_one<kF32, 1, true, kWave>(a, wn, num_sms, balance, smem, stream); break;
+    case 4: launch_one<kF32, 2, false, kWave>(a, wn, num_sms, balance, smem, stream); break;
+    case 5: launch_one<kF32, 2, true, kWave>(a, wn, num_sms, balance, smem, stream); break;
+    case 6: launch_one<kF32, 3, false, kWave>(a, wn, num_sms, balance, smem, stream); break;
+    default: launch_one<kF32, 3, true, kWave>(a, wn, num_sms, balance, smem, stream); break;
     }
 }
 
@@ -901,9 +930,19 @@ void launch_mode(const SubLevelArgs& a, int num_sms, uint32_t balance, size_t sm
 
 int launch_subsample_level(const SubLevelArgs& a, int num_sms, uint32_t balance_blocks, cudaStream_t stream) {
     if (!a.n_nodes) return 0;
-    size_t smem = subsample_smem_bytes();
-    if (a.float_input) launch_mode<true>(a, num_sms, balance_blocks, smem, stream);
-    else launch_mode<false>(a, num_sms, balance_blocks, smem, stream);
+    const size_t smem = subsample_smem_bytes();
+    const WaveNodes none{};
+    if (a.float_input) launch_mode<true, false>(a, none, num_sms, balance_blocks, smem, stream);
+    else launch_mode<false, false>(a, none, num_sms, balance_blocks, smem, stream);
+    return 1;
+}
+
+int launch_subsample_wave(const SubLevelArgs& wave, const WaveNodes& wn, int num_sms, uint32_t balance_blocks,
+                          cudaStream_t stream) {
+    if (!wave.n_nodes) return 0;
+    const size_t smem = subsample_smem_bytes();
+    if (wave.float_input) launch_mode<true, true>(wave, wn, num_sms, balance_blocks, smem, stream);
+    else launch_mode<false, true>(wave, wn, num_sms, balance_blocks, smem, stream);
     return 1;
 }
 

@@ -177,6 +177,17 @@ int launch_prepare_level(SubNode* nodes, uint32_t n_nodes, const uint32_t* out_p
                          uint32_t first_internal, uint64_t* level_base, uint64_t scratch_cap, uint64_t stage_cap,
                          uint32_t* work_counter, uint32_t* err, cudaStream_t stream);
 
+// One subsampling step over the nodes of several builds (a wave): per wave
+// node, the level arguments of its build (`clouds`, indexed by cloud_of),
+// its SubNode and its index in that build's level (for out_points).  The
+// builds share the record type and subsampling mode.
+struct WaveNodes {
+    const SubLevelArgs* clouds;
+    const SubNode* const* node;
+    const uint32_t* cloud_of;
+    const uint32_t* local;
+};
+
 size_t subsample_smem_bytes();
 uint32_t subsample_block_size();
 // balance_blocks: the blocks the level's largest node needs for its share
@@ -184,6 +195,12 @@ uint32_t subsample_block_size();
 // bound x SMs / sum of the bounds); distance-weighted levels size their
 // clusters by it.
 int launch_subsample_level(const SubLevelArgs& a, int num_sms, uint32_t balance_blocks, cudaStream_t stream);
+// `wave` holds what the step shares: n_nodes (all builds' nodes), the work
+// counter, the per-block global brick tables, the mode and record type; the
+// build-specific fields come from wn.clouds.  A node whose build has the
+// capacity error set is skipped.
+int launch_subsample_wave(const SubLevelArgs& wave, const WaveNodes& wn, int num_sms, uint32_t balance_blocks,
+                          cudaStream_t stream);
 
 // Raises a kernel's dynamic shared memory limit on the current device to at
 // least `bytes` and never lowers it, so that builders launching the same
