@@ -373,7 +373,10 @@ def run_batched(args):
 
     def batch_pass():
         t = time.perf_counter()
-        res = octree_api.batch_build(jobs, lanes=args.lanes, memory_budget=args.budget_gb << 30)
+        if args.waves:
+            res = octree_api.batch_build_wave(jobs, wave_size=args.waves, memory_budget=args.budget_gb << 30)
+        else:
+            res = octree_api.batch_build(jobs, lanes=args.lanes, memory_budget=args.budget_gb << 30)
         dt = time.perf_counter() - t
         bad = [r.error.decode() for r in res if r.status != 0]
         if bad:
@@ -403,7 +406,8 @@ def run_batched(args):
         "form": "batched", "ms_per_step": round(b_s * 1e3, 2),
         "config": {"workload": "batched_%d_clouds_50k_4M" % count, "clouds": count, "points": total_pts,
                    "float32_clouds": int((types == 0).sum()), "grids_128_64": int(grid_pick.sum()),
-                   "lanes": args.lanes, "memory_budget_gb": args.budget_gb, "generator_seed": FORM_SEED,
+                   "lanes": args.lanes, "waves": args.waves, "memory_budget_gb": args.budget_gb,
+                   "generator_seed": FORM_SEED,
                    "l2": "inputs larger than L2 (%.1f GB of clouds per step)" % (in_bytes / 1e9)},
         "e2e": {"value": round(total_pts / b_s / 1e6, 3), "unit": "Mpts/s", "h2d_bytes_per_step": in_bytes,
                 "d2h_bytes_per_step": out_bytes, "ms": round(b_s * 1e3, 2)},
@@ -566,6 +570,8 @@ def main():
     ap.add_argument("--lanes", type=int, default=None,
                     help="concurrent builds of the batched and served forms (default 4)")
     ap.add_argument("--budget-gb", type=int, default=150, help="device memory budget of the batched / served forms")
+    ap.add_argument("--waves", type=int, default=0,
+                    help="batched form: build in subsampling waves of this many clouds (ocpi_batch_build_wave)")
     ap.add_argument("--clouds", type=int, default=256, help="clouds of the batched form")
     ap.add_argument("--requests", type=int, default=2000, help="requests of the served form")
     ap.add_argument("--pool", type=int, default=24, help="distinct clouds the served requests draw from")

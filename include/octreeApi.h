@@ -229,6 +229,11 @@ OCPI_EXPORT int ocpi_debug_inject_failures(int kind, uint32_t count);
  * device buffers stay allocated between batches; returns -1 if any failed */
 OCPI_EXPORT int ocpi_batch_build(int device, uint32_t lanes, uint64_t memoryBudget, const OcpiJob* jobs,
                                  uint32_t count, OcpiJobResult* results);
+/* the same batch in subsampling waves: jobs grouped by record type and
+ * subsampling mode, built waveSize at a time on pooled builders, every
+ * subsampling level of a wave in one launch over all its builds */
+OCPI_EXPORT int ocpi_batch_build_wave(int device, uint32_t waveSize, uint64_t memoryBudget, const OcpiJob* jobs,
+                                      uint32_t count, OcpiJobResult* results);
 
 /* ---- allocation-free node subsampling (no counterpart in the reference) --
  *

@@ -19,8 +19,8 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["k_chunking.cu", "k_subsample.cu", "noalloc.cu"]
-CPP_SOURCES = ["builder.cpp", "export.cpp", "octree_api.cpp", "serve.cpp"]
-HEADERS = ["device_common.cuh", "kernels.h", "builder.h"]
+CPP_SOURCES = ["builder.cpp", "export.cpp", "octree_api.cpp", "serve.cpp", "wave.cpp"]
+HEADERS = ["device_common.cuh", "kernels.h", "builder.h", "wave.h"]
 
 LIB = os.path.join(HERE, "libOctreeApi.so")
 SYNTH_LIB = os.path.join(HERE, "libocsynth.so")

@@ -5,6 +5,7 @@
 // reference does on the host in double precision (node bounding boxes,
 // fp_subsampling.cu:15-61, tools.cu:29-61) is done here the same way.
 #include "builder.h"
+#include "wave.h"
 
 #include <algorithm>
 #include <atomic>
@@ -431,6 +432,7 @@ bool Builder::reuse(const BuildConfig& c) {
 }
 
 Builder::~Builder() {
+    if (level_ready_) cudaEventDestroy(level_ready_);
     if (prefetch_stream_) cudaStreamSynchronize(prefetch_stream_);
     if (prefetch_done_) cudaEventDestroy(prefetch_done_);
     if (spare_free_) cudaEventDestroy(spare_free_);
@@ -1144,9 +1146,18 @@ void Builder::subsample() {
         a.global_base = g_base_.as<uint32_t>();
         a.global_cap = g_cap_;
         a.global_shift = g_shift_;
+        // the first pass of a build in a wave meets the wave's other builds
+        // at every level (levels without nodes included); repeats run alone
+        const bool in_wave = wave_ && attempt == 0;
+        if (in_wave && !level_ready_)
+            check_cuda(cudaEventCreateWithFlags(&level_ready_, cudaEventDisableTiming), "event");
+        std::vector<uint64_t> level_bounds;
         for (uint32_t l = 1; l <= depth_; ++l) {
             const uint32_t first = level_first[l], cnt = level_first[l + 1] - first;
-            if (!cnt) continue;
+            if (!cnt) {
+                if (in_wave) wave_->arrive(wave_slot_, l, a, 0, nullptr, g_cap_, level_ready_, stream_);
+                continue;
+            }
             SubNode* lvl = sub_nodes_.as<SubNode>() + first;
             launches_ += launch_prepare_level(lvl, cnt, out_points_.as<uint32_t>(), stage_off_.as<uint64_t>(), first,
                                               level_base_.as<uint64_t>(), scratch_cap, stage_cap,
@@ -1154,7 +1165,14 @@ void Builder::subsample() {
             a.nodes = lvl;
             a.n_nodes = cnt;
             a.out_points = out_points_.as<uint32_t>() + first;
-            launches_ += launch_subsample_level(a, num_sms_, balance[l], stream_);
+            if (in_wave) {
+                level_bounds.resize(cnt);
+                for (uint32_t i = 0; i < cnt; ++i) level_bounds[i] = in_bound[order[first + i]];
+                check_cuda(cudaEventRecord(level_ready_, stream_), "event");
+                wave_->arrive(wave_slot_, l, a, cnt, level_bounds.data(), g_cap_, level_ready_, stream_);
+            } else {
+                launches_ += launch_subsample_level(a, num_sms_, balance[l], stream_);
+            }
             char mark[32];
             std::snprintf(mark, sizeof mark, "sub_l%u", l);
             stage_mark(mark);

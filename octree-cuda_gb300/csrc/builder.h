@@ -144,6 +144,8 @@ bool consume_injected_failure(int kind);
 // Throws the message of the first error bit set in a device error word.
 void throw_device_errors(uint32_t e, const char* stage);
 
+class Wave;
+
 class Builder {
 public:
     // count = true: see upload().
@@ -200,6 +202,13 @@ public:
     // entries when lut != nullptr); capacity in records.  The leaf part is
     // copied while subsampling runs.
     void set_output_host(uint8_t* records, uint32_t* lut, uint64_t capacity);
+    // The subsampling levels of the next builds (their first pass) meet the
+    // other builds of `wave` in slot `slot`: one launch per level over all
+    // of them.  nullptr: the builder subsamples alone.
+    void join_wave(Wave* wave, uint32_t slot) {
+        wave_ = wave;
+        wave_slot_ = slot;
+    }
     bool records_filled(const void* records) const { return host_filled_ && records == host_rec_; }
     bool reused() const { return reuse_tree_; }
     bool lut_filled(const void* lut) const { return host_filled_ && host_lut_ && lut == host_lut_; }
@@ -226,6 +235,9 @@ private:
     BuildConfig cfg_;
     int device_ = 0;
     int num_sms_ = 0;
+    Wave* wave_ = nullptr;
+    uint32_t wave_slot_ = 0;
+    cudaEvent_t level_ready_ = nullptr;   // a level's tables are prepared (waves)
     cudaStream_t stream_ = nullptr;
     uint32_t depth_ = 0;
     std::vector<uint64_t> level_off_;   // pyramid level offsets (cells), depth + 2 entries

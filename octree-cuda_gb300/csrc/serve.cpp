@@ -49,6 +49,7 @@
 
 #include "../../include/octreeApi.h"
 #include "builder.h"
+#include "wave.h"
 
 namespace oc {
 
@@ -624,6 +625,156 @@ Executor* to_executor(void* p) {
 }
 
 }   // namespace
+
+// ---- the batched form in subsampling waves (ocpi_batch_build_wave)
+//
+// Jobs are grouped by record type and subsampling mode (each wave runs one
+// k_subsample instantiation) and, in submission order within a group, built
+// up to `slots` at a time.  Each job of a wave runs on the slot's pooled
+// builder and host thread; their subsampling levels meet in the Wave, one
+// launch per level over all of them.  A wave admits jobs while the slots'
+// envelopes (buffers only grow) stay within the budget; a slot whose
+// envelope keeps a job out frees its builder first.
+struct WavePool {
+    std::mutex run;   // one batch at a time per pool
+    std::unique_ptr<Wave> wave;
+    std::vector<std::unique_ptr<Builder>> builders;
+    std::vector<MemoryTerms> env;
+};
+
+WavePool& wave_pool(int device, uint32_t slots) {
+    static std::mutex mu;
+    static std::map<std::pair<int, uint32_t>, WavePool*> cache;
+    std::lock_guard<std::mutex> g(mu);
+    WavePool*& p = cache[{device, slots}];
+    if (!p) {
+        p = new WavePool;   // kept for the process, like the batch executors
+        int sms = 0;
+        check_cuda(cudaSetDevice(device), "cudaSetDevice");
+        check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "device attribute");
+        p->wave = std::make_unique<Wave>(device, sms);
+        p->builders.resize(slots);
+        p->env.assign(slots, MemoryTerms{});
+    }
+    return *p;
+}
+
+// One job on slot s of the running wave (on its own thread).
+OcpiJobResult run_wave_slot(int device, WavePool& pool, uint32_t s, const OcpiJob& job) {
+    cudaSetDevice(device);
+    const auto t0 = Clock::now();
+    OcpiJobResult r{};
+    std::unique_ptr<Builder>& b = pool.builders[s];
+    try {
+        const BuildConfig cfg = config_of(job);
+        if (!b) b = std::make_unique<Builder>(cfg, job.cloud, device);
+        else b->reconfigure(cfg, job.cloud, false);
+        if (!cfg.has_bbox()) {
+            double real[6], cubic[6];
+            b->compute_bbox(real, cubic);
+        }
+        if (job.outRecords) b->set_output_host(job.outRecords, job.outLut, job.outCapacity);
+        b->join_wave(pool.wave.get(), s);
+        b->generate();
+        b->join_wave(nullptr, 0);
+        const std::vector<uint8_t> hier = b->hierarchy();
+        if (job.outHierarchy) {
+            if (hier.size() > job.outHierarchyCapacity)
+                throw Error("hierarchy output too small: the octree has " + std::to_string(hier.size() / 22) + " nodes");
+            std::memcpy(job.outHierarchy, hier.data(), hier.size());
+        }
+        const Stats& st = b->stats();
+        r.status = 0;
+        r.nodeCount = st.tree_nodes;
+        r.pointsTotal = st.points_total;
+        for (const auto& t : b->timings()) r.deviceMs += t.second;
+    } catch (const std::exception& e) {
+        r.status = -1;
+        std::snprintf(r.error, sizeof r.error, "%s", e.what());
+        b.reset();   // leave no half-finished device state behind
+        pool.env[s] = MemoryTerms{};
+        cudaGetLastError();
+    }
+    pool.wave->leave(s);   // the other builds of the wave stop waiting for this one
+    if (b) b->join_wave(nullptr, 0);
+    r.lane = s;
+    r.runMs = r.totalMs = ms_between(t0, Clock::now());
+    return r;
+}
+
+void run_batch_waves(int device, uint32_t slots, uint64_t budget, const OcpiJob* jobs, uint32_t count,
+                     OcpiJobResult* results) {
+    WavePool& pool = wave_pool(device, slots);
+    std::lock_guard<std::mutex> run(pool.run);
+    int sms = 0;
+    check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "device attribute");
+    std::vector<BuildConfig> cfg(count);
+    std::vector<MemoryTerms> terms(count);
+    std::map<std::tuple<uint32_t, bool, bool, bool, bool>, std::vector<uint32_t>> groups;
+    for (uint32_t i = 0; i < count; ++i) {
+        try {
+            cfg[i] = config_of(jobs[i]);
+            cfg[i].validate();
+            if (!jobs[i].cloud) throw Error("job without a point cloud");
+            terms[i] = memory_terms(cfg[i], sms);
+            if (device_bytes(terms[i]) > budget)
+                throw Error("job needs up to " + std::to_string(device_bytes(terms[i])) +
+                            " device bytes, above the budget of " + std::to_string(budget));
+        } catch (const std::exception& e) {
+            throw Error("job " + std::to_string(i) + " of the batch: " + e.what());
+        }
+        // what selects the k_subsample instantiation (intra wins over inter,
+        // weighting applies with inter only)
+        const BuildConfig& c = cfg[i];
+        const bool inter = !c.intra && c.inter;
+        groups[std::make_tuple(c.cloud_type, c.intra, inter, inter && c.weighting, c.random)].push_back(i);
+    }
+    for (auto& kv : groups) {
+        const std::vector<uint32_t>& ids = kv.second;
+        for (size_t next = 0; next < ids.size();) {
+            // the next wave: jobs in order while every slot's envelope (the
+            // idle slots' too: their builders keep their buffers) fits
+            std::vector<uint32_t> wave;
+            uint64_t used = 0;
+            for (const MemoryTerms& e : pool.env) used += device_bytes(e);
+            auto free_slot = [&](size_t q) {
+                used = used - device_bytes(pool.env[q]) + device_bytes(MemoryTerms{});
+                pool.env[q] = MemoryTerms{};
+                pool.builders[q].reset();
+            };
+            for (size_t s = 0; s < slots && next < ids.size(); ++s) {
+                const uint32_t i = ids[next];
+                MemoryTerms env = envelope(pool.env[s], terms[i]);
+                if (used - device_bytes(pool.env[s]) + device_bytes(env) > budget) {
+                    // this slot's buffers, then those of the idle slots after
+                    // it, make room; the slots before it hold this wave's jobs
+                    free_slot(s);
+                    env = terms[i];
+                    auto fits = [&] { return used - device_bytes(pool.env[s]) + device_bytes(env) <= budget; };
+                    for (size_t q = slots; q-- > s + 1 && !fits();) free_slot(q);
+                    if (!fits()) break;
+                }
+                used += device_bytes(env) - device_bytes(pool.env[s]);
+                pool.env[s] = env;
+                wave.push_back(i);
+                ++next;
+            }
+            if (wave.empty()) throw Error("no job of the batch fits the budget beside the pooled builders");
+            std::vector<uint32_t> depths;
+            for (uint32_t i : wave) {
+                uint32_t d = 0;   // tree depth: log2 of the (validated, power-of-two) chunking grid
+                while ((1u << d) < cfg[i].chunk_grid) ++d;
+                depths.push_back(d);
+            }
+            pool.wave->start(depths);
+            std::vector<std::thread> threads;
+            for (uint32_t s = 0; s < wave.size(); ++s)
+                threads.emplace_back([&, s] { results[wave[s]] = run_wave_slot(device, pool, s, jobs[wave[s]]); });
+            for (auto& t : threads) t.join();
+        }
+    }
+}
+
 }   // namespace oc
 
 extern "C" {
@@ -704,6 +855,18 @@ int ocpi_batch_build(int device, uint32_t lanes, uint64_t memoryBudget, const Oc
             ok = ok && results[i].status == 0;
         }
         if (!ok) throw oc::Error("some builds of the batch failed (see their results)");
+    });
+}
+
+
+int ocpi_batch_build_wave(int device, uint32_t waveSize, uint64_t memoryBudget, const OcpiJob* jobs, uint32_t count,
+                          OcpiJobResult* results) {
+    return oc::guarded([&] {
+        if (!jobs || !results) throw oc::Error("null argument");
+        if (waveSize < 1 || waveSize > 256) throw oc::Error("waveSize must be in [1, 256]");
+        oc::run_batch_waves(device, waveSize, memoryBudget, jobs, count, results);
+        for (uint32_t i = 0; i < count; ++i)
+            if (results[i].status != 0) throw oc::Error("some builds of the batch failed (see their results)");
     });
 }
 

@@ -32,7 +32,8 @@ ADDED_SYMBOLS = [
     "ocpi_get_level_counts", "ocpi_get_timings", "ocpi_subsample_node_noalloc", "ocpi_set_output_host",
     "ocpi_compute_cloud_bb", "ocpi_get_device_memory", "ocpi_estimate_memory",
     "ocpi_server_create", "ocpi_server_destroy", "ocpi_server_submit", "ocpi_server_wait",
-    "ocpi_server_get_hierarchy", "ocpi_server_release", "ocpi_batch_build", "ocpi_server_cancel",
+    "ocpi_server_get_hierarchy", "ocpi_server_release", "ocpi_batch_build", "ocpi_batch_build_wave",
+    "ocpi_server_cancel",
     "ocpi_server_lane_restarts", "ocpi_debug_inject_failures",
 ]
 
@@ -141,6 +142,7 @@ def load_library(path=LIB_PATH):
         "ocpi_server_lane_restarts": [vp, ctypes.POINTER(u64)],
         "ocpi_debug_inject_failures": [ctypes.c_int, u32],
         "ocpi_batch_build": [ctypes.c_int, u32, u64, ctypes.POINTER(OcpiJob), u32, ctypes.POINTER(OcpiJobResult)],
+        "ocpi_batch_build_wave": [ctypes.c_int, u32, u64, ctypes.POINTER(OcpiJob), u32, ctypes.POINTER(OcpiJobResult)],
         "ocpi_estimate_memory": [u32, u32, u8, u32, u32, ctypes.c_float, u32, u32, ctypes.POINTER(u64),
                                  ctypes.POINTER(u64)],
         "ocpi_subsample_node_noalloc": [vp, u8, u32, ctypes.POINTER(d), ctypes.POINTER(d), ctypes.POINTER(d), d,
@@ -441,3 +443,15 @@ def batch_build(jobs, device=0, lanes=4, memory_budget=150 << 30):
     if rc != 0 and all(r.status == 0 for r in res):
         _check(rc, "ocpi_batch_build")   # rejected before any build ran
     return list(res)   # a failed build has status -1 and its message in .error
+
+
+def batch_build_wave(jobs, device=0, wave_size=32, memory_budget=150 << 30):
+    """batch_build in subsampling waves (ocpi_batch_build_wave): jobs of the
+    same record type and mode, wave_size at a time, each subsampling level
+    of a wave in one launch.  Returns the OcpiJobResults."""
+    arr = (OcpiJob * len(jobs))(*jobs)
+    res = (OcpiJobResult * len(jobs))()
+    rc = load_library().ocpi_batch_build_wave(device, wave_size, memory_budget, arr, len(jobs), res)
+    if rc != 0 and all(r.status == 0 for r in res):
+        _check(rc, "ocpi_batch_build_wave")   # rejected before any build ran
+    return list(res)

@@ -68,6 +68,38 @@ def test_batch_equals_builds_alone():
         check_same(w, r, *b)
 
 
+def test_wave_batch_equals_builds_alone():
+    """The batch in subsampling waves (one launch per level over a wave's
+    builds): several record-type and mode groups, waves of 5, some boxes
+    computed on the device; every result equals its build alone."""
+    cases = mixed_cases(14)
+    want = [alone(c, g, m) for c, g, m in cases]
+    bufs = [buffers(w) for w in want]
+    jobs = [job_for(c, g, m, *b, device_bbox=(i % 4 == 0)) for i, ((c, g, m), b) in enumerate(zip(cases, bufs))]
+    results = octree_api.batch_build_wave(jobs, wave_size=5)
+    for w, r, b in zip(want, results, bufs):
+        check_same(w, r, *b)
+
+
+def test_wave_with_a_failing_job():
+    """A job whose box leaves points below it fails in its wave; the wave's
+    other builds do not wait for it and equal their builds alone."""
+    cases = [(c, g, 0) for c, g, _ in mixed_cases(6)]
+    want = [alone(c, g, m) for c, g, m in cases]
+    bufs = [buffers(w) for w in want]
+    jobs = [job_for(c, g, m, *b) for (c, g, m), b in zip(cases, bufs)]
+    bad, g, m = cases[2]
+    shift = (bad.bb_max[0] - bad.bb_min[0]) / 4
+    jobs[2] = octree_api.make_job(bad.cloud, n=bad.n, stride=bad.stride, cloud_type=bad.cloud_type, scale=bad.scale,
+                                  bb_min=[v + shift for v in bad.bb_min], bb_max=[v + shift for v in bad.bb_max],
+                                  chunk_grid=g[0], sub_grid=g[1], merge_threshold=2000, flags=FLAGS[m], seed=99)
+    results = octree_api.batch_build_wave(jobs, wave_size=8)
+    assert results[2].status == -1 and b"below the bounding box" in results[2].error
+    for i, (w, r, b) in enumerate(zip(want, results, bufs)):
+        if i != 2:
+            check_same(w, r, *b)
+
+
 def test_server_admission_under_a_small_budget():
     """A budget that holds about two builds at a time: jobs queue, every one
     completes, results equal the builds alone; an oversized job is refused."""
