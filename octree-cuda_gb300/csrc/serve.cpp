@@ -706,6 +706,7 @@ void run_batch_waves(int device, uint32_t slots, uint64_t budget, const OcpiJob*
                      OcpiJobResult* results) {
     WavePool& pool = wave_pool(device, slots);
     std::lock_guard<std::mutex> run(pool.run);
+    check_cuda(cudaSetDevice(device), "cudaSetDevice");
     int sms = 0;
     check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "device attribute");
     std::vector<BuildConfig> cfg(count);
