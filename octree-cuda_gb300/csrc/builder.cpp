@@ -997,7 +997,10 @@ void Builder::subsample() {
         SubNode& sn = table[k];
         std::memset(&sn, 0, sizeof(sn));
         const double side = cubic / std::pow(2.0, (double)(depth_ - v.level));   // fp_subsampling.cu:16-17
-        const double t = side / S;                                               // kernel_helpers.cuh:14
+        // the node grid's extent is PointCloudInfo::cubicSize of the node box,
+        // max.x - min.x with max.x = min.x + side (fp_subsampling.cu:38-42,
+        // metadata.cuh:66-69); it can differ from side in the last bit
+        const double t = ((v.mn[0] + side) - v.mn[0]) / S;                      // kernel_helpers.cuh:14
         for (int a = 0; a < 3; ++a) {
             sn.ax[a] = make_axis(v.mn[a], t);
             sn.qa[a] = make_qaxis(v.mn[a], cfg_.bb_min[a], 1.0 / cfg_.scale[a], t);

@@ -611,7 +611,9 @@ Result* build(const uint8_t* cloud, const OracleParams& P) {
             const uint32_t vi = list[li];
             const TNode& v = nodes[vi];
             const double side = cubic / std::pow(2.0, (double)(depth - v.level));   // fp_subsampling.cu:16-17
-            const double t = side / Sg;                                           // kernel_helpers.cuh:14
+            // grid extent = cubicSize of the node box: (min.x + side) - min.x
+            // (fp_subsampling.cu:38-42, metadata.cuh:66-69)
+            const double t = ((v.mn[0] + side) - v.mn[0]) / Sg;                  // kernel_helpers.cuh:14
             QAx qa[3] = {make_qax(v.mn[0], P.bb_min[0], sf[0], t), make_qax(v.mn[1], P.bb_min[1], sf[1], t),
                          make_qax(v.mn[2], P.bb_min[2], sf[2], t)};
             std::vector<Cand> cands;
