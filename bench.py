@@ -21,6 +21,7 @@ host cores with all threads.  Multi-GPU runs are independent replicas (the
 path has no exchange step): every rank builds its own cloud.
 """
 import argparse
+import hashlib
 import json
 import os
 import statistics
@@ -179,6 +180,11 @@ def make_cloud(n, threads):
 
 
 def cpu_oracle_time(cloud, bb, n_sample, threads):
+    return cpu_oracle_run(cloud, bb, n_sample, threads)[0]
+
+
+def cpu_oracle_run(cloud, bb, n_sample, threads):
+    """Seconds of one oracle build of the first n_sample points, and its result."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
 
@@ -196,7 +202,37 @@ def cpu_oracle_time(cloud, bb, n_sample, threads):
     dt = time.perf_counter() - t
     if r.stats["error"]:
         raise RuntimeError("oracle failed: %s" % r.stats)
-    return dt
+    return dt, r
+
+
+def link_probe(device, nbytes=1 << 30):
+    """Host link bandwidth in GB/s (best of three 1 GiB pinned copies each
+    way, CUDA events), measured outside every timed region: it tells a slow
+    host link from a slow build in the end-to-end figure."""
+    import torch
+
+    host = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    dev = torch.empty(nbytes, dtype=torch.uint8, device="cuda:%d" % device)
+    out = {}
+    for name, dst, src in (("h2d_gbs", dev, host), ("d2h_gbs", host, dev)):
+        best = None
+        for _ in range(4):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            dst.copy_(src, non_blocking=True)
+            e1.record()
+            e1.synchronize()
+            ms = e0.elapsed_time(e1)
+            best = ms if best is None else min(best, ms)
+        out[name] = round(nbytes / (best * 1e-3) / 1e9, 1)
+    del host, dev
+    return out
+
+
+STAT_KEYS = ["points_total", "p_out", "depth", "tree_nodes", "leaf_nodes", "internal_nodes", "sparse_nodes",
+             "dense_nodes", "max_leaf_depth", "min_leaf_points", "max_leaf_points", "mean_leaf_points",
+             "stdev_leaf_points", "out_capacity"]
 
 
 def run_reference_arm(args):
@@ -638,26 +674,41 @@ def main():
         l2_note = "L2 flushed before every timed build (512 MB write; %.0f MB cloud)" % (cloud_bytes / 1e6)
     else:
         l2_note = "inputs larger than L2 (%.1f GB cloud)" % (cloud_bytes / 1e9)
+    import torch
+
+    torch.cuda.set_device(device)
     clocks = ClockSampler(device)
     clocks.start()
     barrier()
+    torch.cuda.synchronize(device)
     stage_sum = {}
     gen_ms = []
+    step_ms = []
     wall0 = time.perf_counter()
     for _ in range(args.steps):
         if flush is not None:
             flush.zero_()
             torch.cuda.synchronize(device)
+        # ocpi_generate_octree returns when the build's streams are done, so
+        # events on either side of it bracket the whole build, host gaps
+        # included
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
         s.generate()
+        e1.record()
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
         t = s.timings()
         gen_ms.append(sum(t.values()))
         for k, v in t.items():
             stage_sum[k] = stage_sum.get(k, 0.0) + v
+    torch.cuda.synchronize(device)
     barrier()
     wall = time.perf_counter() - wall0
     clk = clocks.stop()
     st = s.stats()
-    ms_step = statistics.mean(gen_ms)
+    ms_step = statistics.mean(step_ms)
     ms_step = replica_max(ms_step, pg)
     value = replicas_throughput(n, ws, ms_step)
     stage_avg = {k: v / args.steps for k, v in stage_sum.items()}
@@ -672,17 +723,20 @@ def main():
     s.set_output_host(recs)
     L = octree_api.load_library()
     init_times = []
-    for i in range(max(2, min(args.steps, 3))):
+    for i in range(args.steps + 1):   # the first is a warm-up of the result arrays
         barrier()
         t0 = time.perf_counter()
         s.init()
-        init_times.append(time.perf_counter() - t0)
+        t1 = time.perf_counter()
         s.generate()
         h = s.hierarchy()
         octree_api._check(L.ocpi_get_records(s._h, recs.ctypes.data), "ocpi_get_records")
-        e2e_times.append(time.perf_counter() - t0)
-    e2e_s = statistics.median(e2e_times)
+        if i:
+            init_times.append(t1 - t0)
+            e2e_times.append(time.perf_counter() - t0)
+    e2e_s = statistics.mean(e2e_times)
     e2e_s = replica_max(e2e_s, pg)
+    link = link_probe(device)
     # ocpi_init_octree inside the end-to-end steps: the chunked upload, with
     # the cloud binned as its chunks land (the call returns when the copy is
     # done)
@@ -723,18 +777,36 @@ def main():
                   "alg_bytes_total": total_alg,
                   "whole_build_gbs": round(total_alg / (ms_step * 1e-3) / 1e9, 1),
                   "tree_nodes": st["tree_nodes"], "internal_nodes": st["internal_nodes"], "p_in": st["p_in"],
-                  "p_out": st["p_out"], "wall_s": round(wall, 3), "upload_ms": upload_ms},
+                  "p_out": st["p_out"], "wall_s": round(wall, 3), "wall_ms_per_step": round(wall * 1e3 / args.steps, 3),
+                  "device_ms_per_step": round(statistics.mean(gen_ms), 3), "upload_ms": upload_ms},
         "e2e": {"value": round(n * ws / e2e_s / 1e6, 3), "unit": "Mpts/s", "h2d_bytes_per_step": n * STRIDE,
-                "d2h_bytes_per_step": hier_bytes + rec_bytes, "ms": round(e2e_s * 1e3, 2)},
+                "d2h_bytes_per_step": hier_bytes + rec_bytes, "ms": round(e2e_s * 1e3, 2),
+                "ms_median": round(statistics.median(e2e_times) * 1e3, 2), "steps": len(e2e_times), **link},
         "clocks": clk,
+        "reference_cuda": {"available": False,
+                           "reason": "the reference's own CUDA pipeline, compiled unmodified for sm_103a, faulted "
+                                     "(illegal memory access) on every cloud it was given on this GPU; it is not "
+                                     "run again"},
     }
     if rank == 0 and not args.no_cpu_baseline:
-        sample = min(CPU_SAMPLE, n)
-        t = cpu_oracle_time(cloud_host, bb, sample, threads)
-        line["cpu_baseline"] = {"value": round(sample / t / 1e6, 3), "unit": "Mpts/s", "cores": threads,
-                                "kind": "port",
-                                "sample": "first %d points of the same cloud, same bbox and settings" % sample}
-    s.close()
+        # the oracle builds the same whole cloud on the host cores; its result
+        # is the check of the GPU build (outside every timed region)
+        hier_gpu = s.hierarchy().tobytes()
+        s.close()
+        t, r = cpu_oracle_run(cloud_host, bb, n, threads)
+        line["cpu_baseline"] = {"value": round(n / t / 1e6, 3), "unit": "Mpts/s", "cores": threads,
+                                "kind": "port", "sample": "the whole %d-point cloud, same bbox and settings" % n}
+        stats_equal = all(st[k] == r.stats[k] for k in STAT_KEYS)
+        line["verified"] = {"by": "CPU oracle, same cloud", "hierarchy_equal": hier_gpu == r.hierarchy.tobytes(),
+                            "stats_equal": stats_equal,
+                            "hierarchy_sha256": hashlib.sha256(hier_gpu).hexdigest(),
+                            "packed_colour_overflow_cells": int(r.stats["guard_color_overflow"]),
+                            "reference_guards": {k: int(r.stats[k]) for k in
+                                                 ("guard_capacity", "guard_truncation", "guard_root_leaf")}}
+        line["verified"]["ok"] = line["verified"]["hierarchy_equal"] and stats_equal
+        del r
+    else:
+        s.close()
     if rank == 0:
         print(json.dumps(line))
     if pg:

@@ -5,10 +5,13 @@
 // reference does on the host in double precision (node bounding boxes,
 // fp_subsampling.cu:15-61, tools.cu:29-61) is done here the same way.
 #include "builder.h"
+
+#include <chrono>
 #include "wave.h"
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -44,7 +47,22 @@ std::atomic<int32_t> g_injected[3];
 void allocation_hook() {
     if (consume_injected_failure(kInjectAllocation)) throw Error("cudaMalloc failed: injected allocation failure");
 }
+
+thread_local AllocTally g_alloc_tally;
+
+// cudaMalloc with the calling thread's tally updated.
+void tallied_malloc(void** p, size_t bytes) {
+    const auto t0 = std::chrono::steady_clock::now();
+    check_cuda(cudaMalloc(p, bytes), "cudaMalloc");
+    g_alloc_tally.ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    g_alloc_tally.events += 1;
+    g_alloc_tally.bytes += bytes;
+}
 }   // namespace
+
+AllocTally& thread_alloc_tally() {
+    return g_alloc_tally;
+}
 
 void inject_failures(int kind, uint32_t count) {
     if (kind != kInjectAllocation && kind != kInjectLaneLoss) throw Error("unknown fault kind");
@@ -73,7 +91,7 @@ void DevBuf::ensure(size_t b) {
     allocation_hook();
     release();
     size_t want = std::max<size_t>(b, 256);
-    check_cuda(cudaMalloc(&p, want), "cudaMalloc");
+    tallied_malloc(&p, want);
     bytes = want;
 }
 
@@ -82,7 +100,7 @@ void DevBuf::ensure_keep(size_t b, size_t keep, cudaStream_t s) {
     allocation_hook();
     size_t want = std::max<size_t>(b + b / 4, 256);
     void* np = nullptr;
-    check_cuda(cudaMalloc(&np, want), "cudaMalloc");
+    tallied_malloc(&np, want);
     if (p && keep) check_cuda(cudaMemcpyAsync(np, p, std::min(keep, bytes), cudaMemcpyDeviceToDevice, s), "grow copy");
     check_cuda(cudaStreamSynchronize(s), "grow sync");
     release();

@@ -58,6 +58,24 @@ struct BuildConfig {
     }
 };
 
+// Device allocations made by the calling thread: host time spent in
+// cudaMalloc, number of allocations and bytes.  The session layer takes the
+// difference around each API call for the statistics report.
+struct AllocTally {
+    double ms = 0;
+    uint64_t events = 0;
+    uint64_t bytes = 0;
+};
+AllocTally& thread_alloc_tally();
+
+// Host-side figures of a session that the statistics report lists beside the
+// build's own: wall time of the API calls (json_exporter.h "process") and the
+// session's device allocations (json_exporter.h "cudamalloc" and "memory").
+struct ReportExtras {
+    std::vector<std::pair<std::string, double>> process_ms;
+    AllocTally allocs;
+};
+
 // Grow-only device allocation.
 struct DevBuf {
     void* p = nullptr;
@@ -187,7 +205,7 @@ public:
     // the uploaded cloud; the cubic box becomes the build's bounding box.
     void compute_bbox(double real[6], double cubic[6]);
     void export_potree(const std::string& dir) const;
-    void export_json_report(const std::string& file) const;
+    void export_json_report(const std::string& file, const ReportExtras& extras) const;
     void export_histogram(const std::string& file, uint32_t bin_width) const;
 
     const Stats& stats() const { return stats_; }

@@ -224,6 +224,13 @@ __device__ __forceinline__ float approx_units(const Coord& c, const AxisGrid& a)
     return __fmul_rn(d, a.r);
 }
 
+// Cell-unit position (p - mn) / t of a coordinate, for distance weighting.
+template <bool kFloatInput>
+__device__ __forceinline__ float point_units(const Coord& c, const AxisGrid& a) {
+    if (kFloatInput || c.ok) return approx_units(c, a);
+    return (float)((c.exact - a.mn) / a.t);
+}
+
 __device__ __forceinline__ int idx_from_units(float x, uint32_t G) {
     if (x >= (float)(G - 1)) return (int)G - 1;
     if (!(x > -1.0f)) return -1;
@@ -349,9 +356,13 @@ __device__ __forceinline__ void decode_colors(uint64_t e, uint16_t& r, uint16_t&
 // Distance weighting.  exp(x) for x in [-15, 0] by Cody & Waite range
 // reduction and the degree-7 Taylor polynomial of e^f (Horner, fused
 // multiply-adds), then exact scaling by 2^k.  The weight of a point at cell
-// units u for neighbour cell n is round(2^20 * exp(-10 * |n + 0.5 - u|^2 * 4/27)),
-// i.e. exp(-10 (d/r)^2) with r the half diagonal of 3x3x3 cells
-// (kernel_inter_cell_filtering.cuh:171-180, fp_subsampling.cu:56-61).
+// units u (its own position, (p - node min) / t, point_units) for neighbour
+// cell n is round(2^28 * exp(-10 * |n + 0.5 - u|^2 * 4/27)), i.e.
+// exp(-10 (d/r)^2) with r the half diagonal of 3x3x3 cells
+// (kernel_inter_cell_filtering.cuh:171-180, fp_subsampling.cu:56-61).  A point
+// lies in its cell, so (d/r)^2 <= 1 and every weight is at least
+// 2^28 e^-10 > 12000: the rounding costs under 1e-4 of a weight.  Sums of
+// weight * colour stay below 2^64 for up to 2^28 colours of at most 255.
 
 __device__ __forceinline__ float exp_neg(float x) {
     const float kLog2e = 1.44269504088896341f;
@@ -380,7 +391,7 @@ __device__ __forceinline__ uint32_t weight_q(float ux, float uy, float uz, int n
     float q = __fmul_rn(d2, (float)(4.0 / 27.0));
     q = fminf(q, 1.5f);
     float w = exp_neg(__fmul_rn(-10.0f, q));
-    return (uint32_t)__fadd_rn(__fmul_rn(w, 1048576.0f), 0.5f);
+    return (uint32_t)__fadd_rn(__fmul_rn(w, 268435456.0f), 0.5f);
 }
 
 // ---------------------------------------------------------------------------

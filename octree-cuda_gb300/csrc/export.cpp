@@ -251,7 +251,7 @@ void Builder::export_potree(const std::string& dir) const {
     write_file(dir + "/metadata.json", text.data(), text.size());
 }
 
-void Builder::export_json_report(const std::string& file) const {
+void Builder::export_json_report(const std::string& file, const ReportExtras& extras) const {
     // statistics.json schema of json_exporter.h:14-99; timings are this
     // session's CUDA-event stage times.
     const Stats& S = stats_;
@@ -275,13 +275,45 @@ void Builder::export_json_report(const std::string& file) const {
     st["pointDistribution"]["stdevPointsPerLeafNode"] = Json::D(S.stdev_leaf_points);
     st["pointDistribution"]["minPointsPerNode"] = Json::U(S.min_leaf_points);
     st["pointDistribution"]["maxPointsPerNode"] = Json::U(S.max_leaf_points);
-    double acc = 0;
+    // the last build's stages: transfers under "memcpy", the rest (kernels on
+    // the build stream) under "kernel"
+    double acc = 0, acc_copy = 0, acc_proc = 0;
+    Json& tm = st["timings"];
+    tm["kernel"] = Json::O();
+    tm["memcpy"] = Json::O();
+    tm["cudamalloc"] = Json::O();
+    tm["process"] = Json::O();
     for (const auto& t : timings_) {
-        st["timings"]["kernel"][t.first]["invocations"] = Json::U(1);
-        st["timings"]["kernel"][t.first]["duration"] = Json::D(t.second);
+        if (t.first == "upload" || t.first == "upload_count" || t.first == "d2h") {
+            tm["memcpy"][t.first] = Json::D(t.second);
+            acc_copy += t.second;
+            continue;
+        }
+        tm["kernel"][t.first]["invocations"] = Json::U(1);
+        tm["kernel"][t.first]["duration"] = Json::D(t.second);
         acc += t.second;
     }
-    st["timings"]["accumulatedKernelTime"] = Json::D(acc);
+    tm["cudamalloc"]["device buffers"] = Json::D(extras.allocs.ms);
+    for (const auto& p : extras.process_ms) {
+        tm["process"][p.first] = Json::D(p.second);
+        acc_proc += p.second;
+    }
+    tm["accumulatedKernelTime"] = Json::D(acc);
+    tm["accumulatedMemCpyTime"] = Json::D(acc_copy);
+    tm["accumulatedMallocTime"] = Json::D(extras.allocs.ms);
+    tm["accumulatedProcessTimings"] = Json::D(acc_proc);
+    // memory (json_exporter.h:88-96): the device allocations this session
+    // holds, the number of allocations it made and their cumulated bytes
+    uint64_t held = 0;
+    Json events = Json::O();
+    for (const auto& a : device_allocations()) {
+        held += a.second;
+        events[a.first] = Json::U(a.second);
+    }
+    st["memory"]["peak"] = Json::U(held);
+    st["memory"]["reserveEvents"] = Json::U(extras.allocs.events);
+    st["memory"]["cumulatedReserved"] = Json::U(extras.allocs.bytes);
+    st["memory"]["events"] = events;
     std::string text;
     dump(st, text, 0);
     write_file(file, text.data(), text.size());

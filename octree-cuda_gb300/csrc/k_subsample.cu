@@ -152,12 +152,6 @@ __device__ __forceinline__ int quant_cell_fine(int32_t q, uint32_t fb, const QAx
     return (i0 == i1 && i0 >= 0) ? i0 : -2;
 }
 
-// Cell-unit position used by distance weighting: the centre of the candidate's
-// quantisation step, ((q - qn) + 1/2) * B + base, in fp32.
-__device__ __forceinline__ float quant_units(int32_t q, const QAxis& a) {
-    return __fmaf_rn(__fadd_rn((float)(q - a.qn), 0.5f), a.B, a.base);
-}
-
 // Position of the k-th set bit (k from 0) of m; k < popcount(m).
 __device__ __forceinline__ uint32_t nth_bit64(uint64_t m, uint32_t k) {
     uint32_t pos = 0;
@@ -505,9 +499,15 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a0, W
                     atomicOr(reinterpret_cast<uint32_t*>(&bm.mask[slot]) + (bit >> 5), 1u << (bit & 31));
                     a.key_cache[off + j] = (slot << 6) | bit;
                     if (weighted) {
-                        a.unit_cache[(off + j) * 3 + 0] = quant_units(q0, qa0);
-                        a.unit_cache[(off + j) * 3 + 1] = quant_units(q1, qa1);
-                        a.unit_cache[(off + j) * 3 + 2] = quant_units(q2, qa2);
+                        // the weight measures the distance from the point itself
+                        // to each neighbour cell centre (kernel_inter_cell_filtering.cuh:171-176)
+                        const uint32_t idx = src_lut[start + k];
+                        Coord co[3];
+                        uint32_t col[3];
+                        load_point<kF32>(a.cloud + (uint64_t)idx * a.stride, co, col);
+                        a.unit_cache[(off + j) * 3 + 0] = point_units<kF32>(co[0], ax0);
+                        a.unit_cache[(off + j) * 3 + 1] = point_units<kF32>(co[1], ax1);
+                        a.unit_cache[(off + j) * 3 + 2] = point_units<kF32>(co[2], ax2);
                     }
                 }
             }

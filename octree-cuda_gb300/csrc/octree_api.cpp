@@ -6,12 +6,14 @@
 // device-side error flags) to UNEXPECTED_ERROR (-1), like the reference's
 // Execute wrapper (octreeApi.cpp:9-21); unlike the reference, CUDA errors do
 // not terminate the process.
+#include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <memory>
 #include <string>
 
 #include "../../include/octreeApi.h"
+
 #include "builder.h"
 
 namespace {
@@ -25,6 +27,7 @@ struct Session {
     const uint8_t* host_cloud = nullptr;
     std::unique_ptr<oc::Builder> builder;
     std::string memory_report;
+    oc::ReportExtras report;   // process times and allocations for statistics.json
     uint8_t* out_rec = nullptr;   // ocpi_set_output_host
     uint32_t* out_lut = nullptr;
     uint64_t out_cap = 0;
@@ -80,6 +83,29 @@ oc::Builder& built(Session* s) {
     if (!s->builder) throw oc::Error("octree not initialised (call ocpi_init_octree)");
     return *s->builder;
 }
+
+// Wall time of one API call and the device allocations it made, recorded in
+// the session's report figures (the reference's TimeTracker "process" entries,
+// session.cpp:62-76, and MemoryTracker events).
+struct ProcessTimer {
+    Session* s;
+    const char* name;
+    std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+    oc::AllocTally before = oc::thread_alloc_tally();
+    ~ProcessTimer() {
+        const oc::AllocTally& now = oc::thread_alloc_tally();
+        s->report.allocs.ms += now.ms - before.ms;
+        s->report.allocs.events += now.events - before.events;
+        s->report.allocs.bytes += now.bytes - before.bytes;
+        const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        for (auto& kv : s->report.process_ms)
+            if (kv.first == name) {
+                kv.second = ms;
+                return;
+            }
+        s->report.process_ms.push_back({name, ms});
+    }
+};
 
 template <class F>
 int execute(F&& fn) {
@@ -203,6 +229,7 @@ int ocpi_configure_subsampling(void* session, uint32_t subsamplingGrid, bool int
 int ocpi_init_octree(void* session) {
     return execute([&] {
         auto* s = to_session(session);
+        ProcessTimer timer{s, "Initialising octree"};
         oc::check_cuda(cudaSetDevice(s->device), "cudaSetDevice");
         if (s->builder && same_config(s->builder->config(), s->cfg)) {
             // same configuration: reuse device state; the upload goes in
@@ -232,6 +259,7 @@ int ocpi_init_octree(void* session) {
 int ocpi_generate_octree(void* session) {
     return execute([&] {
         auto* s = to_session(session);
+        ProcessTimer timer{s, "Generating octree"};
         oc::check_cuda(cudaSetDevice(s->device), "cudaSetDevice");
         built(s).generate();
     });
@@ -240,14 +268,17 @@ int ocpi_generate_octree(void* session) {
 int ocpi_export_potree(void* session, const char* directory) {
     return execute([&] {
         if (!directory) throw oc::Error("null directory");
-        built(to_session(session)).export_potree(directory);
+        auto* s = to_session(session);
+        ProcessTimer timer{s, "Exporting octree"};
+        built(s).export_potree(directory);
     });
 }
 
 int ocpi_export_json_report(void* session, const char* filename) {
     return execute([&] {
         if (!filename) throw oc::Error("null filename");
-        built(to_session(session)).export_json_report(filename);
+        auto* s = to_session(session);
+        built(s).export_json_report(filename, s->report);
     });
 }
 

@@ -35,13 +35,17 @@
 //                         Distance weighting (kernel_inter_cell_filtering.cuh:109-194,
 //                         float atomics in the reference) -> fixed-point integer
 //                         accumulation of an fp32 weight, see weight_q below.
+//                         F_WEIGHT_LITERAL instead restates the reference's own
+//                         arithmetic (binary64 distances, float exp, float sums
+//                         in one fixed order, truncating division): the yardstick
+//                         for the +-1 tolerance of the canonical rule.
 //   * export              breathFirstExport potree_exporter.cu:62-96
 //   * statistics          OctreeData::updateNodeStatistics octree.cu:79-132
 //
 // The exact cell / coordinate formulas are evaluated directly in double here.
 // The only fp32 quantity the oracle shares with the GPU path is the cell-unit
-// position used by distance weighting (quant_units: the centre of the point's
-// quantisation step in the node's grid), which is part of the canonical
+// position used by distance weighting (point_units: (p - node min) / t from a
+// float-pair split of the coordinate), which is part of the canonical
 // definition of the weighted mode.
 
 #include <algorithm>
@@ -73,7 +77,18 @@ struct OracleParams {
     uint32_t reserved;
 };
 
-enum : uint32_t { F_INTRA = 1, F_INTER = 2, F_REPLACE = 4, F_RANDOM = 8, F_WEIGHT = 16 };
+enum : uint32_t {
+    F_INTRA = 1,
+    F_INTER = 2,
+    F_REPLACE = 4,
+    F_RANDOM = 8,
+    F_WEIGHT = 16,
+    // test variants of distance weighting (the canonical rule is F_WEIGHT alone):
+    F_WEIGHT_LITERAL = 32,   // the reference's float arithmetic, propagated up the levels
+    F_WEIGHT_LOCAL = 64,     // with LITERAL: each node's literal colours from the canonical
+                             // children's colours; the canonical colours propagate
+    F_WEIGHT_REVERSE = 128,  // with LITERAL: float sums in the reverse candidate order
+};
 
 #pragma pack(push, 1)
 struct Record {   // OutputBuffer, types.cuh:18-24
@@ -210,29 +225,59 @@ inline int32_t ref_out_coord(double p, double mn, double sf) {
 // ---------------------------------------------------------------------------
 // Shared canonical pieces (must match the GPU path bit for bit).
 
-// Quantised-coordinate parameters of one node axis: qn = quantised coordinate
-// of the node minimum, base = ((cloud_min - node_min) + qn / sf) / t and
-// B = 1 / (sf t) rounded to float; evaluated in this operation order.
-struct QAx {
-    int32_t qn;
-    float base;
-    float B;
+// Cell-unit position (p - mn) / t of a coordinate, as the GPU path evaluates
+// it: the coordinate split into a float pair hi + lo (float input: hi = p,
+// lo = 0; double input: hi = p with its mantissa cut to 24 bits, lo = the
+// rest rounded to float), the node minimum likewise (m_hi = float(mn),
+// m_lo = float(mn - m_hi)), then ((hi - m_hi) + (lo - m_lo)) * float(1 / t).
+struct UAx {
+    double mn, t;
+    float m_hi, m_lo, r;
 };
 
-inline QAx make_qax(double node_min, double cloud_min, double sf, double t) {
-    QAx q;
-    double qn = std::floor((node_min - cloud_min) * sf);
-    q.qn = (int32_t)qn;
-    double base = ((cloud_min - node_min) + (double)q.qn / sf) / t;
-    q.base = (float)base;
-    q.B = (float)(1.0 / (sf * t));
-    return q;
+inline UAx make_uax(double mn, double t) {
+    UAx a;
+    a.mn = mn;
+    a.t = t;
+    a.m_hi = (float)mn;
+    a.m_lo = (float)(mn - (double)a.m_hi);
+    a.r = (float)(1.0 / t);
+    return a;
 }
 
-// Cell-unit position of a point with quantised coordinate q (its output
-// record coordinate): the centre of its quantisation step, in fp32.
-inline float quant_units(int32_t q, const QAx& a) {
-    return std::fmaf((float)(q - a.qn) + 0.5f, a.B, a.base);
+inline float point_units(double p, bool f32, const UAx& a) {
+    float hi, lo;
+    if (f32) {
+        hi = (float)p;
+        lo = 0.0f;
+    } else {
+        uint64_t bits;
+        std::memcpy(&bits, &p, 8);
+        const uint32_t e = (uint32_t)(bits >> 52) & 0x7FFu;
+        const uint64_t mant = bits & ((1ull << 52) - 1);
+        const uint32_t sign = (uint32_t)(bits >> 63) << 31;
+        if (e == 0 && mant == 0) {
+            std::memcpy(&hi, &sign, 4);
+            lo = 0.0f;
+        } else {
+            const int ue = (int)e - 1023;
+            if (ue < -60 || ue > 100) return (float)((p - a.mn) / a.t);
+            const uint32_t hb = sign | ((uint32_t)(ue + 127) << 23) | (uint32_t)(mant >> 29);
+            std::memcpy(&hi, &hb, 4);
+            const uint32_t low = (uint32_t)(mant & ((1u << 29) - 1));
+            if (low == 0) {
+                lo = 0.0f;
+            } else {
+                const uint32_t sb = (uint32_t)(ue - 52 + 127) << 23;
+                float sc;
+                std::memcpy(&sc, &sb, 4);
+                const float lf = (float)low * sc;
+                lo = sign ? -lf : lf;
+            }
+        }
+    }
+    const float d = (hi - a.m_hi) + (lo - a.m_lo);
+    return d * a.r;
 }
 
 // exp(x) for x in [-15, 0]: Cody & Waite range reduction x = k*ln2 + f with
@@ -265,7 +310,7 @@ inline float exp_neg(float x) {
 //   d2 = |(n + 0.5) - u|^2 in cell units, (d / r)^2 = d2 * 4/27 with
 //   r = half diagonal of 3x3x3 cells (fp_subsampling.cu:56-61),
 //   w = exp(-10 (d/r)^2) (kernel_inter_cell_filtering.cuh:176-180),
-//   wq = round(w * 2^20).
+//   wq = round(w * 2^28), at least 2^28 e^-10 > 12000 for a point in its cell.
 inline uint32_t weight_q(const float u[3], int32_t nx, int32_t ny, int32_t nz) {
     float dx = ((float)nx + 0.5f) - u[0];
     float dy = ((float)ny + 0.5f) - u[1];
@@ -274,7 +319,7 @@ inline uint32_t weight_q(const float u[3], int32_t nx, int32_t ny, int32_t nz) {
     float q = d2 * (float)(4.0 / 27.0);
     q = std::fmin(q, 1.5f);
     float w = exp_neg(-10.0f * q);
-    return (uint32_t)(w * 1048576.0f + 0.5f);
+    return (uint32_t)(w * 268435456.0f + 0.5f);
 }
 
 inline void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
@@ -587,6 +632,9 @@ Result* build(const uint8_t* cloud, const OracleParams& P) {
     const bool intra = (P.flags & F_INTRA) != 0;
     const bool inter = !intra && (P.flags & F_INTER) != 0;
     const bool weighted = inter && (P.flags & F_WEIGHT) != 0;
+    const bool literal = weighted && (P.flags & F_WEIGHT_LITERAL) != 0;
+    const bool local = literal && (P.flags & F_WEIGHT_LOCAL) != 0;
+    const bool reverse = literal && (P.flags & F_WEIGHT_REVERSE) != 0;
     const bool random = (P.flags & F_RANDOM) != 0;
     // reference launch extent per child slot: maxPointsPerNode * 8 threads in
     // 128-thread blocks, fp_subsampling.cuh:317-330
@@ -600,6 +648,7 @@ Result* build(const uint8_t* cloud, const OracleParams& P) {
     }
     std::vector<std::vector<uint32_t>> out_idx(nodes.size());
     std::vector<std::vector<std::array<uint16_t, 3>>> out_col(nodes.size());
+    std::vector<std::vector<std::array<uint16_t, 3>>> out_col_lit(local ? nodes.size() : 0);
     std::vector<uint32_t> by_level[32];
     for (size_t i = 0; i < nodes.size(); ++i)
         if (nodes[i].internal) by_level[nodes[i].level].push_back((uint32_t)i);
@@ -614,8 +663,7 @@ Result* build(const uint8_t* cloud, const OracleParams& P) {
             // grid extent = cubicSize of the node box: (min.x + side) - min.x
             // (fp_subsampling.cu:38-42, metadata.cuh:66-69)
             const double t = ((v.mn[0] + side) - v.mn[0]) / Sg;                  // kernel_helpers.cuh:14
-            QAx qa[3] = {make_qax(v.mn[0], P.bb_min[0], sf[0], t), make_qax(v.mn[1], P.bb_min[1], sf[1], t),
-                         make_qax(v.mn[2], P.bb_min[2], sf[2], t)};
+            const UAx ua[3] = {make_uax(v.mn[0], t), make_uax(v.mn[1], t), make_uax(v.mn[2], t)};
             std::vector<Cand> cands;
             cands.reserve(v.sub_count);
             for (int s = 0; s < 8; ++s) {
@@ -655,7 +703,7 @@ Result* build(const uint8_t* cloud, const OracleParams& P) {
                     cd.key = (uint32_t)(ix + iy * Sg + iz * (uint64_t)Sg * Sg);
                     if (weighted)
                         for (int a = 0; a < 3; ++a)
-                            cd.u[a] = quant_units(ref_out_coord(p[a], P.bb_min[a], sf[a]), qa[a]);
+                            cd.u[a] = point_units(p[a], P.cloud_type == 0, ua[a]);
                     cands.push_back(cd);
                 }
             }
@@ -697,6 +745,7 @@ Result* build(const uint8_t* cloud, const OracleParams& P) {
             };
             std::vector<uint64_t> inter_sum;
             std::vector<std::array<uint64_t, 4>> wacc;
+            std::vector<std::array<float, 4>> facc;
             if (inter && !weighted) {
                 inter_sum.assign(C, 0);
                 for (size_t j = 0; j < C; ++j) {
@@ -719,7 +768,41 @@ Result* build(const uint8_t* cloud, const OracleParams& P) {
                     if (cntn >= 1024 || sr > 0xFFFF || sg > 0xFFFF || sb > 0xFFFF) ++over;
                 }
             }
-            if (weighted) {
+            if (literal) {
+                // The reference's own arithmetic, kernelInterCellAvgWeighted
+                // (kernel_inter_cell_filtering.cuh:137-189): binary64 distance
+                // from the point to the neighbour cell centre over the half
+                // diagonal diag_3_3_half (fp_subsampling.cu:56-61), float exp,
+                // float sums (here in one fixed order: candidates by cell, then
+                // cloud index, neighbours x-major), output (u16)(sum / weight)
+                // (fp_subsampling.cuh:209-217).
+                facc.assign(C, {0.f, 0.f, 0.f, 0.f});
+                const double diag = std::pow((t * 3) * (t * 3) * 3, 0.5) / 2.0;
+                for (size_t kk = 0; kk < cands.size(); ++kk) {
+                    const Cand& cd = cands[reverse ? cands.size() - 1 - kk : kk];
+                    double p[3];
+                    uint16_t raw[3];
+                    load_point(cloud + (uint64_t)cd.idx * P.stride, P.cloud_type, p, raw);
+                    int64_t x = cd.key % Sg, y = (cd.key / Sg) % Sg, z = cd.key / ((uint64_t)Sg * Sg);
+                    for (int ox = -1; ox <= 1; ++ox)
+                        for (int oy = -1; oy <= 1; ++oy)
+                            for (int oz = -1; oz <= 1; ++oz) {
+                                int64_t n = find_cell(x + ox, y + oy, z + oz);
+                                if (n < 0) continue;
+                                const int32_t nx = (int32_t)(x + ox), ny = (int32_t)(y + oy), nz = (int32_t)(z + oz);
+                                const double dx = (v.mn[0] + nx * t + (t * 0.5)) - p[0];
+                                const double dy = (v.mn[1] + ny * t + (t * 0.5)) - p[1];
+                                const double dz = (v.mn[2] + nz * t + (t * 0.5)) - p[2];
+                                float res = static_cast<float>(std::sqrt(dx * dx + dy * dy + dz * dz) / diag);
+                                res = std::exp(-((res * res) * 10.f));
+                                facc[n][0] += static_cast<float>(cd.c[0]) * res;
+                                facc[n][1] += static_cast<float>(cd.c[1]) * res;
+                                facc[n][2] += static_cast<float>(cd.c[2]) * res;
+                                facc[n][3] += res;
+                            }
+                }
+            }
+            if (weighted && (!literal || local)) {
                 wacc.assign(C, {0, 0, 0, 0});
                 for (size_t k = 0; k < cands.size(); ++k) {
                     const Cand& cd = cands[k];
@@ -757,7 +840,14 @@ Result* build(const uint8_t* cloud, const OracleParams& P) {
                 uint16_t col[3];
                 if (intra) decode_colors(intra_sum[j], col, &div0);
                 else if (weighted) {
-                    for (int a = 0; a < 3; ++a) col[a] = (uint16_t)(wacc[j][a] / wacc[j][3]);
+                    if (literal && !local)
+                        for (int a = 0; a < 3; ++a) col[a] = static_cast<uint16_t>(facc[j][a] / facc[j][3]);
+                    else
+                        for (int a = 0; a < 3; ++a) col[a] = (uint16_t)(wacc[j][a] / wacc[j][3]);
+                    if (local)
+                        out_col_lit[vi].push_back({static_cast<uint16_t>(facc[j][0] / facc[j][3]),
+                                                   static_cast<uint16_t>(facc[j][1] / facc[j][3]),
+                                                   static_cast<uint16_t>(facc[j][2] / facc[j][3])});
                 } else if (inter) decode_colors(inter_sum[j], col, &div0);
                 else {
                     double p[3];
@@ -814,7 +904,7 @@ Result* build(const uint8_t* cloud, const OracleParams& P) {
         const TNode& v = nodes[ni];
         if (!v.internal) return;
         const auto& oi = out_idx[ni];
-        const auto& oc = out_col[ni];
+        const auto& oc = local ? out_col_lit[ni] : out_col[ni];
         for (size_t j = 0; j < oi.size(); ++j) {
             double p[3];
             uint16_t raw[3];

@@ -18,6 +18,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 
 F_INTRA, F_INTER, F_REPLACE, F_RANDOM, F_WEIGHT = 1, 2, 4, 8, 16
+# test variants of distance weighting (oracle.cpp): the reference's float
+# arithmetic propagated up the levels, per node only, and with reversed sums
+F_WEIGHT_LITERAL, F_WEIGHT_LOCAL, F_WEIGHT_REVERSE = 32, 64, 128
 
 
 class OracleParams(ctypes.Structure):

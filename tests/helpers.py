@@ -80,6 +80,12 @@ def flags_of(cfg):
         f |= oracle.F_RANDOM
     if cfg.get("weighting"):
         f |= oracle.F_WEIGHT
+    if cfg.get("weight_literal"):
+        f |= oracle.F_WEIGHT_LITERAL
+    if cfg.get("weight_local"):
+        f |= oracle.F_WEIGHT_LOCAL
+    if cfg.get("weight_reverse"):
+        f |= oracle.F_WEIGHT_REVERSE
     return f
 
 

@@ -298,3 +298,184 @@ def test_potree_export_reader(tmp_path):
         a = int(hier["byte_offset"][i]) // 18
         p = xyz[a: a + int(hier["points"][i])]
         assert (p >= mins[i] - 2 * scale).all() and (p <= mins[i] + sides[i] + 2 * scale).all(), i
+
+
+def test_reference_reader_reads_export(tmp_path):
+    """The reference's own Potree reader (tools/potree_to_ply.py:51-248,
+    standard-library Python; staged into oracle/_ref/tools by
+    oracle/build_ref.py) reads this library's export: it walks hierarchy.bin
+    breadth first, reads every node's byte range of octree.bin and writes one
+    PLY file per level plus one of all leaves.  Each file must hold exactly
+    the records of its level's nodes, in breadth-first order."""
+    import re
+    import subprocess
+    import sys
+
+    import build_ref
+
+    reader = build_ref.reader()
+    if reader is None:
+        pytest.skip("reference reader not staged (oracle/build_ref.py)")
+    case = make_case(0, 0, 400_000, seed=73)
+    cfg = dict(chunk_grid=128, sub_grid=64, merge_threshold=3000, inter=True)
+    s = run_gpu(case, cfg)
+    out = tmp_path / "potree"
+    out.mkdir()
+    s.export_potree(str(out))
+    hier = s.hierarchy()
+    recs = s.records()
+    s.close()
+    ply = tmp_path / "ply"
+    ply.mkdir()
+    r = subprocess.run([sys.executable, reader, "-i", str(out) + "/", "-o", str(ply)], capture_output=True,
+                       text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    counts = [int(v) for v in re.findall(r"Exported points: (\d+)", r.stdout)]
+    # node levels from the breadth-first masks
+    level = np.zeros(len(hier), np.int64)
+    nxt = 1
+    for i in range(len(hier)):
+        for _ in range(bin(int(hier["mask"][i])).count("1")):
+            level[nxt] = level[i] + 1
+            nxt += 1
+    assert nxt == len(hier)
+    depth = int(level.max()) + 1
+    assert len(counts) == depth + 1
+    raw = recs.view(np.uint8).reshape(-1, 18)
+
+    def node_bytes(idx):
+        parts = [raw[int(hier["byte_offset"][i]) // 18: int(hier["byte_offset"][i]) // 18 + int(hier["points"][i])]
+                 for i in idx]
+        return np.concatenate(parts).tobytes() if parts else b""
+
+    def ply_body(name):
+        data = (ply / name).read_bytes()
+        head, body = data.split(b"end_header\n", 1)
+        n = int(re.search(rb"element vertex (\d+)", head).group(1))
+        assert len(body) == 18 * n
+        return n, body
+
+    for lv in range(depth):
+        idx = np.nonzero(level == lv)[0]
+        n, body = ply_body("converted_level_%d.ply" % lv)
+        assert n == counts[lv] == int(hier["points"][idx].sum())
+        assert body == node_bytes(idx), lv
+    leaves = np.nonzero(hier["mask"] == 0)[0]
+    n, body = ply_body("converted_level_leaf.ply")
+    assert n == counts[-1] == case.n
+    assert body == node_bytes(leaves)
+
+
+# statistics.json of OctreeApi/src/json_exporter.h:14-99: top-level keys in
+# order, and the keys of each section ("averaging" only with averaging)
+STATISTICS_SCHEMA = {
+    "depth": None,
+    "chunking": ["grid", "mergingThreshold"],
+    "subsampling": ["grid", "strategy", "averaging"],
+    "resultNodes": ["octreeNodes", "leafNodeAmount", "internalNodeAmount", "maxLeafDepth"],
+    "overallNodes": ["sparseOctreeNodes", "denseOctreeNodes", "memorySaving"],
+    "pointDistribution": ["meanPointsPerLeafNode", "stdevPointsPerLeafNode", "minPointsPerNode", "maxPointsPerNode"],
+    "timings": ["kernel", "memcpy", "cudamalloc", "process", "accumulatedKernelTime", "accumulatedMemCpyTime",
+                "accumulatedMallocTime", "accumulatedProcessTimings"],
+    "memory": ["peak", "reserveEvents", "cumulatedReserved", "events"],
+}
+
+
+@pytest.mark.parametrize("mode", [dict(inter=True), dict(random=True)])
+def test_statistics_json_schema(tmp_path, mode):
+    """ocpi_export_json_report keeps the reference's statistics.json schema,
+    with the build's node statistics, stage and process timings and device
+    allocations."""
+    import json
+
+    case = make_case(1, 0, 300_000, seed=75)
+    cfg = dict(chunk_grid=128, sub_grid=64, merge_threshold=3000, **mode)
+    ref = run_oracle(case, cfg)
+    s = run_gpu(case, cfg)
+    s.export_potree(str(tmp_path))
+    path = tmp_path / "statistics.json"
+    s.export_json_report(str(path))
+    used = s.device_memory()
+    s.close()
+    st = json.loads(path.read_text())
+    assert list(st.keys()) == list(STATISTICS_SCHEMA)
+    for k, keys in STATISTICS_SCHEMA.items():
+        if keys is None:
+            continue
+        want = [x for x in keys if x != "averaging" or mode.get("inter") or mode.get("intra")]
+        assert list(st[k].keys()) == want, k
+    S = ref.stats
+    assert st["depth"] == S["depth"]
+    assert st["chunking"] == {"grid": 128, "mergingThreshold": 3000}
+    assert st["subsampling"]["strategy"] == ("EXPLICIT RANDOM SUBSAMPLING" if mode.get("random")
+                                             else "IMPLICIT RANDOM SUBSAMPLING")
+    assert st["resultNodes"] == {"octreeNodes": S["leaf_nodes"] + S["internal_nodes"], "leafNodeAmount": S["leaf_nodes"],
+                                 "internalNodeAmount": S["internal_nodes"], "maxLeafDepth": S["max_leaf_depth"]}
+    assert st["overallNodes"]["sparseOctreeNodes"] == S["sparse_nodes"]
+    assert st["overallNodes"]["denseOctreeNodes"] == S["dense_nodes"]
+    pd = st["pointDistribution"]
+    assert pd["minPointsPerNode"] == S["min_leaf_points"] and pd["maxPointsPerNode"] == S["max_leaf_points"]
+    assert pd["meanPointsPerLeafNode"] == pytest.approx(S["mean_leaf_points"], rel=1e-6)
+    tm = st["timings"]
+    assert "upload_count" in tm["memcpy"] or "upload" in tm["memcpy"]
+    assert all(v["duration"] >= 0 and v["invocations"] == 1 for v in tm["kernel"].values())
+    assert tm["accumulatedKernelTime"] == pytest.approx(sum(v["duration"] for v in tm["kernel"].values()), rel=1e-5)
+    assert set(tm["process"]) == {"Initialising octree", "Generating octree", "Exporting octree"}
+    assert tm["accumulatedMallocTime"] > 0
+    mem = st["memory"]
+    assert mem["peak"] == used == sum(mem["events"].values())
+    assert mem["reserveEvents"] > 0 and mem["cumulatedReserved"] >= mem["peak"]
+
+
+def test_distribution_histogram(tmp_path):
+    """ocpi_export_distribution_histogram writes the point-distribution page of
+    octree_processor_impl/histogram.cu:39-119: the reference's automatic bin
+    width (3.5 stdev / leaves^(1/3), in float), bins from the smallest leaf,
+    every leaf counted once.  The reference sizes its bins so that the
+    largest leaf falls one bin past the end of its vector (histogram.cu:58-63);
+    this library adds that bin."""
+    import math
+    import re
+
+    case = make_case(0, 0, 600_000, seed=77)
+    cfg = dict(chunk_grid=256, sub_grid=64, merge_threshold=2000, inter=True)
+    s = run_gpu(case, cfg)
+    st = s.stats()
+    path = tmp_path / "hist.html"
+    s.export_histogram(str(path), 0)
+    html = path.read_text()
+    width = int(re.search(r"binWidth\((\d+)\)", html).group(1))
+    f32 = np.float32
+    expect = math.ceil(f32(3.5) * (f32(st["stdev_leaf_points"]) / f32(st["leaf_nodes"]) ** f32(1.0 / 3.0)))
+    assert width == max(1, expect)
+    data = [int(v) for v in re.search(r"data:\[([0-9,]*)\]", html).group(1).split(",")]
+    assert sum(data) == st["leaf_nodes"]
+    hier = s.hierarchy()
+    pts = hier["points"][hier["mask"] == 0].astype(np.int64)
+    bins = np.minimum((pts - st["min_leaf_points"]) // width, len(data) - 1)
+    assert np.array_equal(np.bincount(bins, minlength=len(data)), data)
+    assert "mergingThreshold(2000), points(%d)" % case.n in html
+    s.export_histogram(str(path), 50)
+    assert "binWidth(50)" in path.read_text()
+    s.close()
+
+
+# The plain workloads at full size: seeded clouds of the reference datasets'
+# sizes (coin 5,138,448 float; heidentor 25,836,417 float), grids 512/128.
+FULL_SIZE = {
+    "A_5M_f32_inter": (0, 0, 5_138_448, 20240602, 0.001, dict(inter=True)),
+    "B1_26M_f32_random_intra": (1, 0, 25_836_417, 20240603, 0.001, dict(random=True, intra=True)),
+    "B2_26M_f32_random_inter_weighted": (1, 0, 25_836_417, 20240603, 0.001,
+                                          dict(random=True, inter=True, weighting=True)),
+}
+
+
+@pytest.mark.parametrize("name", sorted(FULL_SIZE))
+def test_workloads_full_size(name):
+    kind, cloud_type, n, seed, scale, modes = FULL_SIZE[name]
+    case = make_case(kind, cloud_type, n, seed=seed, scale=scale)
+    cfg = dict(chunk_grid=512, sub_grid=128, merge_threshold=10000, output_factor=2.2, **modes)
+    ref = run_oracle(case, cfg)
+    s = run_gpu(case, cfg)
+    compare_results(ref, s)
+    s.close()

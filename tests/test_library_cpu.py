@@ -132,3 +132,100 @@ def test_fault_injection_kinds():
     assert b"unknown fault kind" in L.ocpi_last_error()
     assert L.ocpi_debug_inject_failures(octree_api.INJECT_ALLOCATION, 0) == 0
     assert L.ocpi_debug_inject_failures(octree_api.INJECT_LANE_LOSS, 0) == 0
+
+
+# The reference CLI's call sequence (src/main.cpp:54-107): a session, the
+# cloud setters, the two configuration calls, init, generate, export and the
+# three reports, then destroy.
+CALLER = r"""
+#include <stdio.h>
+#include <string.h>
+#include "octreeApi.h"
+
+int main(int argc, char** argv)
+{
+    const char* out = argc > 1 ? argv[1] : ".";
+    static unsigned char cloud[15 * 4];
+    char path[4096];
+    void* session = 0;
+    int rc[19], k = 0;
+    rc[k++] = ocpi_set_logging_level(1);
+    rc[k++] = ocpi_create_session(&session, 0);
+    rc[k++] = ocpi_set_cloud_type(session, 0);
+    rc[k++] = ocpi_set_cloud_point_amount(session, 4);
+    rc[k++] = ocpi_set_cloud_data_stride(session, 15);
+    rc[k++] = ocpi_set_cloud_scale(session, 0.001, 0.001, 0.001);
+    rc[k++] = ocpi_set_cloud_offset(session, 0.0, 0.0, 0.0);
+    rc[k++] = ocpi_set_cloud_bb(session, 0.0, 0.0, 0.0, 1.0, 1.0, 1.0);
+    rc[k++] = ocpi_set_point_cloud_host(session, cloud);
+    rc[k++] = ocpi_configure_chunking(session, 512, 10000, 2.2f);
+    rc[k++] = ocpi_configure_subsampling(session, 128, 0, 1, 1, 0, 0);
+    rc[k++] = ocpi_init_octree(session);
+    rc[k++] = ocpi_generate_octree(session);
+    rc[k++] = ocpi_export_potree(session, out);
+    snprintf(path, sizeof path, "%s/point_distribution.html", out);
+    rc[k++] = ocpi_export_distribution_histogram(session, path, 0);
+    snprintf(path, sizeof path, "%s/statistics.json", out);
+    rc[k++] = ocpi_export_json_report(session, path);
+    snprintf(path, sizeof path, "%s/memory_report.html", out);
+    rc[k++] = ocpi_export_memory_report(session, path);
+    rc[k++] = ocpi_destroy_session(session);
+    for (int i = 0; i < k; ++i) printf("%d ", rc[i]);
+    printf("\n%s\n", ocpi_last_error ? "linked" : "");
+    return 0;
+}
+"""
+
+
+def _compile_and_run(tmp_path, compiler, source, include_dir, lang):
+    import shutil
+    import subprocess
+
+    cc = shutil.which(compiler)
+    if not cc:
+        pytest.skip("no %s" % compiler)
+    lib_dir = os.path.dirname(octree_api.LIB_PATH)
+    src = tmp_path / ("caller." + lang)
+    src.write_text(source)
+    exe = tmp_path / "caller"
+    subprocess.run([cc, "-I", include_dir, str(src), "-o", str(exe), "-L", lib_dir, "-lOctreeApi",
+                    "-Wl,-rpath," + lib_dir], check=True)
+    r = subprocess.run([str(exe), str(tmp_path)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    return [int(v) for v in r.stdout.split("\n")[0].split()]
+
+
+def _check_codes(codes):
+    assert len(codes) == 18
+    assert codes[0] == 0   # logging level
+    try:
+        import torch
+
+        gpu = torch.cuda.is_available()
+    except ImportError:
+        gpu = False
+    if not gpu:
+        # no device: the session cannot be created, and every call on the
+        # missing session returns UNEXPECTED_ERROR instead of faulting
+        assert codes[1] == -1
+        assert all(c == -1 for c in codes[2:]), codes
+
+
+def test_c_caller_links_and_runs(tmp_path):
+    """A C program making the reference CLI's calls compiles against
+    include/octreeApi.h (as C11), links against libOctreeApi.so and runs."""
+    codes = _compile_and_run(tmp_path, "gcc", "#include <stdbool.h>\n" + CALLER,
+                             os.path.join(ROOT, "include"), "c")
+    _check_codes(codes)
+
+
+def test_caller_against_reference_header_links(tmp_path):
+    """The same caller compiled as C++ against the reference's own declarations
+    (OctreeApi/include/octreeApi.h, whose EXPORTED macro is extern "C" on this
+    platform) resolves every call in libOctreeApi.so."""
+    ref_inc = os.path.join(os.environ.get("OC_REFERENCE_DIR", "/root/reference"), "OctreeApi", "include")
+    if not os.path.exists(os.path.join(ref_inc, "octreeApi.h")):
+        pytest.skip("reference checkout not present")
+    src = CALLER.replace('printf("\\n%s\\n", ocpi_last_error ? "linked" : "");', 'printf("\\nlinked\\n");')
+    codes = _compile_and_run(tmp_path, "g++", src, ref_inc, "cpp")
+    _check_codes(codes)
