@@ -781,7 +781,9 @@ def main():
                   "device_ms_per_step": round(statistics.mean(gen_ms), 3), "upload_ms": upload_ms},
         "e2e": {"value": round(n * ws / e2e_s / 1e6, 3), "unit": "Mpts/s", "h2d_bytes_per_step": n * STRIDE,
                 "d2h_bytes_per_step": hier_bytes + rec_bytes, "ms": round(e2e_s * 1e3, 2),
-                "ms_median": round(statistics.median(e2e_times) * 1e3, 2), "steps": len(e2e_times), **link},
+                "ms_median": round(statistics.median(e2e_times) * 1e3, 2), "steps": len(e2e_times),
+                "step_ms": [round(x * 1e3, 2) for x in e2e_times],
+                "init_ms": [round(x * 1e3, 2) for x in init_times], **link},
         "clocks": clk,
         "reference_cuda": {"available": False,
                            "reason": "the reference's own CUDA pipeline, compiled unmodified for sm_103a, faulted "

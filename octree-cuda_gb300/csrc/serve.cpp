@@ -635,6 +635,11 @@ Executor* to_executor(void* p) {
 // launch per level over all of them.  A wave admits jobs while the slots'
 // envelopes (buffers only grow) stay within the budget; a slot whose
 // envelope keeps a job out frees its builder first.
+// One pool per device, kept for the process like the batch executors: a
+// batch's builders and the wave's buffers stay allocated for the next batch.
+// Between batches the pool holds its slots' builders (their envelopes, in
+// `env`) and the wave's buffers; admission counts both.  A batch with fewer
+// slots than the pool frees the builders of the slots it does not use.
 struct WavePool {
     std::mutex run;   // one batch at a time per pool
     std::unique_ptr<Wave> wave;
@@ -642,30 +647,28 @@ struct WavePool {
     std::vector<MemoryTerms> env;
 };
 
-WavePool& wave_pool(int device, uint32_t slots) {
+WavePool& wave_pool(int device) {
     static std::mutex mu;
-    static std::map<std::pair<int, uint32_t>, WavePool*> cache;
+    static std::map<int, WavePool*> cache;
     std::lock_guard<std::mutex> g(mu);
-    WavePool*& p = cache[{device, slots}];
+    WavePool*& p = cache[device];
     if (!p) {
-        p = new WavePool;   // kept for the process, like the batch executors
+        p = new WavePool;
         int sms = 0;
         check_cuda(cudaSetDevice(device), "cudaSetDevice");
         check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "device attribute");
         p->wave = std::make_unique<Wave>(device, sms);
-        p->builders.resize(slots);
-        p->env.assign(slots, MemoryTerms{});
     }
     return *p;
 }
 
 // One job on slot s of the running wave (on its own thread).
 OcpiJobResult run_wave_slot(int device, WavePool& pool, uint32_t s, const OcpiJob& job) {
-    cudaSetDevice(device);
     const auto t0 = Clock::now();
     OcpiJobResult r{};
     std::unique_ptr<Builder>& b = pool.builders[s];
     try {
+        check_cuda(cudaSetDevice(device), "cudaSetDevice");
         const BuildConfig cfg = config_of(job);
         if (!b) b = std::make_unique<Builder>(cfg, job.cloud, device);
         else b->reconfigure(cfg, job.cloud, false);
@@ -704,9 +707,15 @@ OcpiJobResult run_wave_slot(int device, WavePool& pool, uint32_t s, const OcpiJo
 
 void run_batch_waves(int device, uint32_t slots, uint64_t budget, const OcpiJob* jobs, uint32_t count,
                      OcpiJobResult* results) {
-    WavePool& pool = wave_pool(device, slots);
+    WavePool& pool = wave_pool(device);
     std::lock_guard<std::mutex> run(pool.run);
     check_cuda(cudaSetDevice(device), "cudaSetDevice");
+    if (pool.builders.size() > slots) {
+        pool.builders.resize(slots);   // frees the builders of the slots this batch does not use
+        pool.env.resize(slots);
+    }
+    pool.builders.resize(slots);
+    pool.env.resize(slots, MemoryTerms{});
     int sms = 0;
     check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "device attribute");
     std::vector<BuildConfig> cfg(count);
@@ -736,7 +745,17 @@ void run_batch_waves(int device, uint32_t slots, uint64_t budget, const OcpiJob*
             // the next wave: jobs in order while every slot's envelope (the
             // idle slots' too: their builders keep their buffers) fits
             std::vector<uint32_t> wave;
-            uint64_t used = 0;
+            // the wave's own buffers: what it holds, or what this wave's
+            // largest possible jobs need, whichever is more
+            uint64_t wave_nodes = 0;
+            uint32_t wave_gcap = 0;
+            for (size_t q = next, k = 0; q < ids.size() && k < slots; ++q, ++k) {
+                wave_nodes += terms[ids[q]].node_cap;
+                wave_gcap = std::max<uint32_t>(wave_gcap, (uint32_t)terms[ids[q]].slots);
+            }
+            const uint64_t wave_bytes =
+                std::max(pool.wave->device_bytes(), Wave::bytes_for(sms, slots, wave_nodes, wave_gcap));
+            uint64_t used = wave_bytes;
             for (const MemoryTerms& e : pool.env) used += device_bytes(e);
             auto free_slot = [&](size_t q) {
                 used = used - device_bytes(pool.env[q]) + device_bytes(MemoryTerms{});
@@ -767,7 +786,13 @@ void run_batch_waves(int device, uint32_t slots, uint64_t budget, const OcpiJob*
                 while ((1u << d) < cfg[i].chunk_grid) ++d;
                 depths.push_back(d);
             }
-            pool.wave->start(depths);
+            uint64_t max_nodes = 0;
+            uint32_t max_gcap = 0;
+            for (uint32_t i : wave) {
+                max_nodes += terms[i].node_cap;
+                max_gcap = std::max<uint32_t>(max_gcap, (uint32_t)terms[i].slots);
+            }
+            pool.wave->start(depths, max_nodes, max_gcap);
             std::vector<std::thread> threads;
             for (uint32_t s = 0; s < wave.size(); ++s)
                 threads.emplace_back([&, s] { results[wave[s]] = run_wave_slot(device, pool, s, jobs[wave[s]]); });
