@@ -406,11 +406,21 @@ def run_batched(args):
         return time.perf_counter() - t
 
     jobs = [form_job(c, g, m, r, h) for c, g, m, r, h in zip(clouds, grids, modes, recs, hiers)]
+    tuning = None
+    tune_s = None
+    if args.waves == "auto":
+        # the autotuner's trials run on a sample of this batch, outside the
+        # timed region
+        t0 = time.perf_counter()
+        tuning = octree_api.batch_autotune(jobs, memory_budget=args.budget_gb << 30, sample_jobs=48)
+        tune_s = time.perf_counter() - t0
 
     def batch_pass():
         t = time.perf_counter()
-        if args.waves:
-            res = octree_api.batch_build_wave(jobs, wave_size=args.waves, memory_budget=args.budget_gb << 30)
+        if tuning is not None:
+            res = octree_api.batch_build_tuned(jobs, tuning, memory_budget=args.budget_gb << 30)
+        elif args.waves != "lanes":
+            res = octree_api.batch_build_wave(jobs, wave_size=int(args.waves), memory_budget=args.budget_gb << 30)
         else:
             res = octree_api.batch_build(jobs, lanes=args.lanes, memory_budget=args.budget_gb << 30)
         dt = time.perf_counter() - t
@@ -442,7 +452,10 @@ def run_batched(args):
         "form": "batched", "ms_per_step": round(b_s * 1e3, 2),
         "config": {"workload": "batched_%d_clouds_50k_4M" % count, "clouds": count, "points": total_pts,
                    "float32_clouds": int((types == 0).sum()), "grids_128_64": int(grid_pick.sum()),
-                   "lanes": args.lanes, "waves": args.waves, "memory_budget_gb": args.budget_gb,
+                   "lanes": args.lanes if args.waves == "lanes" else None, "waves": args.waves,
+                   "tuning": tuning.as_dict() if tuning is not None else None,
+                   "autotune_s": round(tune_s, 2) if tune_s is not None else None,
+                   "memory_budget_gb": args.budget_gb,
                    "generator_seed": FORM_SEED,
                    "l2": "inputs larger than L2 (%.1f GB of clouds per step)" % (in_bytes / 1e9)},
         "e2e": {"value": round(total_pts / b_s / 1e6, 3), "unit": "Mpts/s", "h2d_bytes_per_step": in_bytes,
@@ -606,8 +619,10 @@ def main():
     ap.add_argument("--lanes", type=int, default=None,
                     help="concurrent builds of the batched and served forms (default 4)")
     ap.add_argument("--budget-gb", type=int, default=150, help="device memory budget of the batched / served forms")
-    ap.add_argument("--waves", type=int, default=0,
-                    help="batched form: build in subsampling waves of this many clouds (ocpi_batch_build_wave)")
+    ap.add_argument("--waves", default="auto",
+                    help="batched form: 'auto' (subsampling waves with the autotuned size, cluster caps and graph "
+                         "capture: ocpi_batch_autotune + ocpi_batch_build_tuned), a wave size "
+                         "(ocpi_batch_build_wave), or 'lanes' (the lane executor, ocpi_batch_build)")
     ap.add_argument("--clouds", type=int, default=256, help="clouds of the batched form")
     ap.add_argument("--requests", type=int, default=2000, help="requests of the served form")
     ap.add_argument("--pool", type=int, default=24, help="distinct clouds the served requests draw from")

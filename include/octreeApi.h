@@ -230,10 +230,38 @@ OCPI_EXPORT int ocpi_debug_inject_failures(int kind, uint32_t count);
 OCPI_EXPORT int ocpi_batch_build(int device, uint32_t lanes, uint64_t memoryBudget, const OcpiJob* jobs,
                                  uint32_t count, OcpiJobResult* results);
 /* the same batch in subsampling waves: jobs grouped by record type and
- * subsampling mode, built waveSize at a time on pooled builders, every
- * subsampling level of a wave in one launch over all its builds */
+ * subsampling mode, built waveSize at a time on pooled builders; each wave's
+ * subsampling, every level of all its builds with one launch per level, is
+ * captured into one CUDA graph.  waveSize 0: the tuning that
+ * ocpi_batch_autotune chose for a batch like this one, autotuning on this
+ * batch first when there is none */
 OCPI_EXPORT int ocpi_batch_build_wave(int device, uint32_t waveSize, uint64_t memoryBudget, const OcpiJob* jobs,
                                       uint32_t count, OcpiJobResult* results);
+
+/* Tuning of the batched form in waves. */
+typedef struct OcpiBatchTuning {
+    uint32_t waveSize;            /* builds per wave, 1..256 */
+    uint32_t clusterCap;          /* largest thread-block cluster per node of a subsampling level: 1, 2, 4 or 8 */
+    uint32_t weightedClusterCap;  /* the same for distance-weighted levels: 1..16 (above 8 non-portable) */
+    uint32_t useGraphs;           /* 1: each wave's subsampling schedule is captured into one CUDA graph */
+    double trialMs;               /* ocpi_batch_autotune: measured time of this choice on its sample */
+    uint32_t trials;              /* ocpi_batch_autotune: configurations measured */
+    uint32_t lastIssue;           /* set by the library: 1 if the last wave ran as one graph launch */
+} OcpiBatchTuning;
+
+/* Measures ocpi_batch_build_wave on an evenly spaced sample of the jobs (at
+ * most sampleJobs of them, 0: 48; their output arrays are written) over a
+ * sweep of wave sizes, cluster caps and graph capture, and returns the
+ * fastest in `tuning`.  The choice is kept for the rest of the process per
+ * device and batch signature (job count, mean size, share of float64 clouds,
+ * of distance-weighted jobs and of 512-grid jobs, each in buckets); with a
+ * cachePath it is also read from and appended to that text file, so that a
+ * later process starts tuned. */
+OCPI_EXPORT int ocpi_batch_autotune(int device, uint64_t memoryBudget, const OcpiJob* jobs, uint32_t count,
+                                    uint32_t sampleJobs, const char* cachePath, OcpiBatchTuning* tuning);
+/* ocpi_batch_build_wave with an explicit tuning; tuning->lastIssue is set */
+OCPI_EXPORT int ocpi_batch_build_tuned(int device, uint64_t memoryBudget, OcpiBatchTuning* tuning,
+                                       const OcpiJob* jobs, uint32_t count, OcpiJobResult* results);
 
 /* ---- allocation-free node subsampling (no counterpart in the reference) --
  *

@@ -1167,36 +1167,53 @@ void Builder::subsample() {
         a.global_base = g_base_.as<uint32_t>();
         a.global_cap = g_cap_;
         a.global_shift = g_shift_;
-        // the first pass of a build in a wave meets the wave's other builds
-        // at every level (levels without nodes included); repeats run alone
+        // the first pass of a build in a wave hands its whole plan to the
+        // wave, which issues it with the other builds' (one subsampling
+        // launch per level over all of them); repeats run alone
         const bool in_wave = wave_ && attempt == 0;
-        if (in_wave && !level_ready_)
-            check_cuda(cudaEventCreateWithFlags(&level_ready_, cudaEventDisableTiming), "event");
-        std::vector<uint64_t> level_bounds;
-        for (uint32_t l = 1; l <= depth_; ++l) {
-            const uint32_t first = level_first[l], cnt = level_first[l + 1] - first;
-            if (!cnt) {
-                if (in_wave) wave_->arrive(wave_slot_, l, a, 0, nullptr, g_cap_, level_ready_, stream_);
-                continue;
+        if (in_wave) {
+            if (!level_ready_) check_cuda(cudaEventCreateWithFlags(&level_ready_, cudaEventDisableTiming), "event");
+            std::vector<WaveLevel> plan(depth_);
+            for (uint32_t l = 1; l <= depth_; ++l) {
+                const uint32_t first = level_first[l], cnt = level_first[l + 1] - first;
+                WaveLevel& w = plan[l - 1];
+                w.a = a;
+                w.a.n_nodes = cnt;
+                if (!cnt) continue;
+                SubNode* lvl = sub_nodes_.as<SubNode>() + first;
+                w.a.nodes = lvl;
+                w.a.out_points = out_points_.as<uint32_t>() + first;
+                w.bounds.resize(cnt);
+                for (uint32_t i = 0; i < cnt; ++i) w.bounds[i] = in_bound[order[first + i]];
+                uint32_t* outp = out_points_.as<uint32_t>();
+                uint64_t* soff = stage_off_.as<uint64_t>();
+                uint64_t* lbase = level_base_.as<uint64_t>();
+                uint32_t* work = work_.as<uint32_t>();
+                uint32_t* err = err_.as<uint32_t>();
+                w.prepare = [=](cudaStream_t st) {
+                    launch_prepare_level(lvl, cnt, outp, soff, first, lbase, scratch_cap, stage_cap, work, err, st);
+                };
+                ++launches_;
             }
-            SubNode* lvl = sub_nodes_.as<SubNode>() + first;
-            launches_ += launch_prepare_level(lvl, cnt, out_points_.as<uint32_t>(), stage_off_.as<uint64_t>(), first,
-                                              level_base_.as<uint64_t>(), scratch_cap, stage_cap,
-                                              work_.as<uint32_t>(), err_.as<uint32_t>(), stream_);
-            a.nodes = lvl;
-            a.n_nodes = cnt;
-            a.out_points = out_points_.as<uint32_t>() + first;
-            if (in_wave) {
-                level_bounds.resize(cnt);
-                for (uint32_t i = 0; i < cnt; ++i) level_bounds[i] = in_bound[order[first + i]];
-                check_cuda(cudaEventRecord(level_ready_, stream_), "event");
-                wave_->arrive(wave_slot_, l, a, cnt, level_bounds.data(), g_cap_, level_ready_, stream_);
-            } else {
+            check_cuda(cudaEventRecord(level_ready_, stream_), "event");
+            wave_->submit(wave_slot_, std::move(plan), g_cap_, level_ready_, stream_);
+            stage_mark("subsample");
+        } else {
+            for (uint32_t l = 1; l <= depth_; ++l) {
+                const uint32_t first = level_first[l], cnt = level_first[l + 1] - first;
+                if (!cnt) continue;
+                SubNode* lvl = sub_nodes_.as<SubNode>() + first;
+                launches_ += launch_prepare_level(lvl, cnt, out_points_.as<uint32_t>(), stage_off_.as<uint64_t>(),
+                                                  first, level_base_.as<uint64_t>(), scratch_cap, stage_cap,
+                                                  work_.as<uint32_t>(), err_.as<uint32_t>(), stream_);
+                a.nodes = lvl;
+                a.n_nodes = cnt;
+                a.out_points = out_points_.as<uint32_t>() + first;
                 launches_ += launch_subsample_level(a, num_sms_, balance[l], stream_);
+                char mark[32];
+                std::snprintf(mark, sizeof mark, "sub_l%u", l);
+                stage_mark(mark);
             }
-            char mark[32];
-            std::snprintf(mark, sizeof mark, "sub_l%u", l);
-            stage_mark(mark);
         }
         // internal nodes' records to their post-order positions
         launches_ += launch_place_prepare(post_ii_.as<uint32_t>(), n_internal, out_points_.as<uint32_t>(),

@@ -868,10 +868,11 @@ uint32_t cluster_size(uint32_t n_nodes, int num_sms, uint32_t cap) {
 
 template <bool kF32, int kColor, bool kRandom, bool kWave>
 void launch_one(const SubLevelArgs& a, const WaveNodes& wn, int num_sms, uint32_t balance, size_t smem,
-                cudaStream_t stream) {
-    uint32_t cs = cluster_size(a.n_nodes, num_sms, kColor == 3 ? 16u : 4u);
+                cudaStream_t stream, const ClusterCaps& caps) {
+    const uint32_t cap = kColor == 3 ? caps.weighted : caps.plain;
+    uint32_t cs = cluster_size(a.n_nodes, num_sms, cap);
     if (kColor == 3)
-        while (cs < 16 && cs < balance) cs <<= 1;
+        while (cs < cap && cs < balance) cs <<= 1;
     if (cs > 1) {
         auto kern = k_subsample<kF32, kColor, kRandom, true, kWave>;
         allow_dynamic_smem(reinterpret_cast<const void*>(kern), smem);
@@ -908,21 +909,21 @@ void launch_one(const SubLevelArgs& a, const WaveNodes& wn, int num_sms, uint32_
 
 template <bool kF32, bool kWave>
 void launch_mode(const SubLevelArgs& a, const WaveNodes& wn, int num_sms, uint32_t balance, size_t smem,
-                 cudaStream_t stream) {
+                 cudaStream_t stream, const ClusterCaps& caps) {
     const bool intra = (a.mode & kModeIntra) != 0;
     const bool inter = !intra && (a.mode & kModeInter) != 0;
     const bool weighted = inter && (a.mode & kModeWeight) != 0;
     const int color = intra ? 1 : (weighted ? 3 : (inter ? 2 : 0));
     const bool random = (a.mode & kModeRandom) != 0;
     switch (color * 2 + (random ? 1 : 0)) {
-    case 0: launch_one<kF32, 0, false, kWave>(a, wn, num_sms, balance, smem, stream); break;
-    case 1: launch_one<kF32, 0, true, kWave>(a, wn, num_sms, balance, smem, stream); break;
-    case 2: launch_one<kF32, 1, false, kWave>(a, wn, num_sms, balance, smem, stream); break;
-    case 3: launch_one<kF32, 1, true, kWave>(a, wn, num_sms, balance, smem, stream); break;
-    case 4: launch_one<kF32, 2, false, kWave>(a, wn, num_sms, balance, smem, stream); break;
-    case 5: launch_one<kF32, 2, true, kWave>(a, wn, num_sms, balance, smem, stream); break;
-    case 6: launch_one<kF32, 3, false, kWave>(a, wn, num_sms, balance, smem, stream); break;
-    default: launch_one<kF32, 3, true, kWave>(a, wn, num_sms, balance, smem, stream); break;
+    case 0: launch_one<kF32, 0, false, kWave>(a, wn, num_sms, balance, smem, stream, caps); break;
+    case 1: launch_one<kF32, 0, true, kWave>(a, wn, num_sms, balance, smem, stream, caps); break;
+    case 2: launch_one<kF32, 1, false, kWave>(a, wn, num_sms, balance, smem, stream, caps); break;
+    case 3: launch_one<kF32, 1, true, kWave>(a, wn, num_sms, balance, smem, stream, caps); break;
+    case 4: launch_one<kF32, 2, false, kWave>(a, wn, num_sms, balance, smem, stream, caps); break;
+    case 5: launch_one<kF32, 2, true, kWave>(a, wn, num_sms, balance, smem, stream, caps); break;
+    case 6: launch_one<kF32, 3, false, kWave>(a, wn, num_sms, balance, smem, stream, caps); break;
+    default: launch_one<kF32, 3, true, kWave>(a, wn, num_sms, balance, smem, stream, caps); break;
     }
 }
 
@@ -932,17 +933,18 @@ int launch_subsample_level(const SubLevelArgs& a, int num_sms, uint32_t balance_
     if (!a.n_nodes) return 0;
     const size_t smem = subsample_smem_bytes();
     const WaveNodes none{};
-    if (a.float_input) launch_mode<true, false>(a, none, num_sms, balance_blocks, smem, stream);
-    else launch_mode<false, false>(a, none, num_sms, balance_blocks, smem, stream);
+    const ClusterCaps caps{};
+    if (a.float_input) launch_mode<true, false>(a, none, num_sms, balance_blocks, smem, stream, caps);
+    else launch_mode<false, false>(a, none, num_sms, balance_blocks, smem, stream, caps);
     return 1;
 }
 
 int launch_subsample_wave(const SubLevelArgs& wave, const WaveNodes& wn, int num_sms, uint32_t balance_blocks,
-                          cudaStream_t stream) {
+                          cudaStream_t stream, const ClusterCaps& caps) {
     if (!wave.n_nodes) return 0;
     const size_t smem = subsample_smem_bytes();
-    if (wave.float_input) launch_mode<true, true>(wave, wn, num_sms, balance_blocks, smem, stream);
-    else launch_mode<false, true>(wave, wn, num_sms, balance_blocks, smem, stream);
+    if (wave.float_input) launch_mode<true, true>(wave, wn, num_sms, balance_blocks, smem, stream, caps);
+    else launch_mode<false, true>(wave, wn, num_sms, balance_blocks, smem, stream, caps);
     return 1;
 }
 

@@ -199,8 +199,14 @@ int launch_subsample_level(const SubLevelArgs& a, int num_sms, uint32_t balance_
 // counter, the per-block global brick tables, the mode and record type; the
 // build-specific fields come from wn.clouds.  A node whose build has the
 // capacity error set is skipped.
+// Largest thread-block cluster per node of a subsampling level: unweighted
+// modes, and distance-weighted ones (clusters above 8 are non-portable).
+struct ClusterCaps {
+    uint32_t plain = 4;
+    uint32_t weighted = 16;
+};
 int launch_subsample_wave(const SubLevelArgs& wave, const WaveNodes& wn, int num_sms, uint32_t balance_blocks,
-                          cudaStream_t stream);
+                          cudaStream_t stream, const ClusterCaps& caps = ClusterCaps{});
 
 // Raises a kernel's dynamic shared memory limit on the current device to at
 // least `bytes` and never lowers it, so that builders launching the same

@@ -35,13 +35,16 @@
 // kernel is deterministic up to the order of records inside a node.
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <condition_variable>
 #include <cstdio>
 #include <cstring>
 #include <deque>
+#include <fstream>
 #include <map>
 #include <memory>
 #include <mutex>
+#include <sstream>
 #include <string>
 #include <thread>
 #include <tuple>
@@ -705,11 +708,14 @@ OcpiJobResult run_wave_slot(int device, WavePool& pool, uint32_t s, const OcpiJo
     return r;
 }
 
-void run_batch_waves(int device, uint32_t slots, uint64_t budget, const OcpiJob* jobs, uint32_t count,
-                     OcpiJobResult* results) {
+void run_batch_waves(int device, const OcpiBatchTuning& tuning, uint64_t budget, const OcpiJob* jobs, uint32_t count,
+                     OcpiJobResult* results, int* last_issue) {
+    const uint32_t slots = tuning.waveSize;
     WavePool& pool = wave_pool(device);
     std::lock_guard<std::mutex> run(pool.run);
     check_cuda(cudaSetDevice(device), "cudaSetDevice");
+    pool.wave->set_graphs(tuning.useGraphs != 0);
+    pool.wave->set_cluster_caps(ClusterCaps{tuning.clusterCap, tuning.weightedClusterCap});
     if (pool.builders.size() > slots) {
         pool.builders.resize(slots);   // frees the builders of the slots this batch does not use
         pool.env.resize(slots);
@@ -797,8 +803,158 @@ void run_batch_waves(int device, uint32_t slots, uint64_t budget, const OcpiJob*
             for (uint32_t s = 0; s < wave.size(); ++s)
                 threads.emplace_back([&, s] { results[wave[s]] = run_wave_slot(device, pool, s, jobs[wave[s]]); });
             for (auto& t : threads) t.join();
+            if (last_issue) *last_issue = pool.wave->last_issue();
         }
     }
+}
+
+// ---- autotuning of the batched form
+//
+// A batch's signature puts it in a bucket: log2 of the job count and of the
+// mean point count, and in tenths the shares of float64 clouds, of
+// distance-weighted jobs and of jobs on grids above 256.  For a signature the
+// tuner measures the batch form on an evenly spaced sample of the batch:
+// first the wave sizes with the default caps and graphs, then the cluster
+// caps at the best wave size, then graph capture off, and keeps the fastest.
+// The first trial runs twice and only its second run counts (buffers grow on
+// the first).
+
+namespace {
+
+std::string batch_signature(int device, const OcpiJob* jobs, uint32_t count) {
+    cudaDeviceProp prop{};
+    cudaGetDeviceProperties(&prop, device);
+    double pts = 0;
+    uint32_t f64 = 0, weighted = 0, big = 0;
+    for (uint32_t i = 0; i < count; ++i) {
+        pts += jobs[i].pointAmount;
+        f64 += jobs[i].cloudType == 1;
+        const uint32_t m = jobs[i].modeFlags;
+        weighted += !(m & OCPI_SUB_INTRA) && (m & OCPI_SUB_INTER) && (m & OCPI_SUB_WEIGHTING);
+        big += jobs[i].chunkingGrid > 256;
+    }
+    auto lg = [](double v) { return v >= 1 ? (int)std::floor(std::log2(v)) : 0; };
+    auto tenth = [&](uint32_t c) { return count ? (int)(10.0 * c / count + 0.5) : 0; };
+    char buf[512];
+    std::snprintf(buf, sizeof buf, "%s/%d/jobs2^%d/pts2^%d/f64:%d/w:%d/g512:%d", prop.name, prop.multiProcessorCount,
+                  lg(count), lg(count ? pts / count : 0), tenth(f64), tenth(weighted), tenth(big));
+    for (char* c = buf; *c; ++c)
+        if (*c == ' ') *c = '_';
+    return buf;
+}
+
+std::mutex g_tuned_mu;
+std::map<std::string, OcpiBatchTuning> g_tuned;
+
+bool load_tuning(const char* path, const std::string& sig, OcpiBatchTuning& t) {
+    if (!path) return false;
+    std::ifstream f(path);
+    std::string line;
+    bool found = false;
+    while (std::getline(f, line)) {   // the last entry of a signature wins
+        std::istringstream in(line);
+        std::string key;
+        OcpiBatchTuning v{};
+        if (in >> key >> v.waveSize >> v.clusterCap >> v.weightedClusterCap >> v.useGraphs >> v.trialMs >> v.trials &&
+            key == sig) {
+            t = v;
+            found = true;
+        }
+    }
+    return found;
+}
+
+void store_tuning(const char* path, const std::string& sig, const OcpiBatchTuning& t) {
+    if (!path) return;
+    std::ofstream f(path, std::ios::app);
+    f << sig << ' ' << t.waveSize << ' ' << t.clusterCap << ' ' << t.weightedClusterCap << ' ' << t.useGraphs << ' '
+      << t.trialMs << ' ' << t.trials << '\n';
+}
+
+void validate_tuning(const OcpiBatchTuning& t) {
+    if (t.waveSize < 1 || t.waveSize > 256) throw Error("waveSize must be in [1, 256]");
+    if (t.clusterCap < 1 || t.clusterCap > 8 || (t.clusterCap & (t.clusterCap - 1)))
+        throw Error("clusterCap must be 1, 2, 4 or 8");
+    if (t.weightedClusterCap < 1 || t.weightedClusterCap > 16 || (t.weightedClusterCap & (t.weightedClusterCap - 1)))
+        throw Error("weightedClusterCap must be a power of two up to 16");
+}
+
+OcpiBatchTuning default_tuning() {
+    OcpiBatchTuning t{};
+    t.waveSize = 32;
+    t.clusterCap = 4;
+    t.weightedClusterCap = 16;
+    t.useGraphs = 1;
+    return t;
+}
+
+}   // namespace
+
+OcpiBatchTuning autotune(int device, uint64_t budget, const OcpiJob* jobs, uint32_t count, uint32_t sample_jobs,
+                         const char* cache_path) {
+    if (!count) throw Error("empty batch");
+    const std::string sig = batch_signature(device, jobs, count);
+    OcpiBatchTuning best{};
+    {
+        std::lock_guard<std::mutex> g(g_tuned_mu);
+        auto it = g_tuned.find(sig);
+        if (it != g_tuned.end()) return it->second;
+        if (load_tuning(cache_path, sig, best)) {
+            validate_tuning(best);
+            g_tuned[sig] = best;
+            return best;
+        }
+    }
+    const uint32_t m = std::min<uint32_t>(count, sample_jobs ? sample_jobs : 48);
+    std::vector<OcpiJob> sample(m);
+    for (uint32_t k = 0; k < m; ++k) sample[k] = jobs[(uint64_t)k * count / m];
+    std::vector<OcpiJobResult> res(m);
+    uint32_t trials = 0;
+    auto measure = [&](const OcpiBatchTuning& t) {
+        const auto t0 = Clock::now();
+        run_batch_waves(device, t, budget, sample.data(), m, res.data(), nullptr);
+        const double ms = ms_between(t0, Clock::now());
+        for (const auto& r : res)
+            if (r.status != 0) throw Error(std::string("autotune trial failed: ") + r.error);
+        ++trials;
+        return ms;
+    };
+    best = default_tuning();
+    best.waveSize = std::min<uint32_t>(best.waveSize, m);
+    measure(best);   // buffers grow on the first run
+    best.trialMs = measure(best);
+    auto consider = [&](OcpiBatchTuning t) {
+        if (t.waveSize == best.waveSize && t.clusterCap == best.clusterCap &&
+            t.weightedClusterCap == best.weightedClusterCap && t.useGraphs == best.useGraphs)
+            return;
+        t.trialMs = measure(t);
+        if (t.trialMs < best.trialMs) best = t;
+    };
+    for (uint32_t w : {8u, 16u, 32u, 64u}) {
+        if (w > m) continue;
+        OcpiBatchTuning t = best;
+        t.waveSize = w;
+        consider(t);
+    }
+    const OcpiBatchTuning at_size = best;
+    for (auto caps : {std::make_pair(2u, 8u), std::make_pair(8u, 16u), std::make_pair(4u, 8u)}) {
+        OcpiBatchTuning t = at_size;
+        t.clusterCap = caps.first;
+        t.weightedClusterCap = caps.second;
+        consider(t);
+    }
+    {
+        OcpiBatchTuning t = best;
+        t.useGraphs = 0;
+        consider(t);
+    }
+    best.trials = trials;
+    {
+        std::lock_guard<std::mutex> g(g_tuned_mu);
+        g_tuned[sig] = best;
+    }
+    store_tuning(cache_path, sig, best);
+    return best;
 }
 
 }   // namespace oc
@@ -889,8 +1045,32 @@ int ocpi_batch_build_wave(int device, uint32_t waveSize, uint64_t memoryBudget, 
                           OcpiJobResult* results) {
     return oc::guarded([&] {
         if (!jobs || !results) throw oc::Error("null argument");
-        if (waveSize < 1 || waveSize > 256) throw oc::Error("waveSize must be in [1, 256]");
-        oc::run_batch_waves(device, waveSize, memoryBudget, jobs, count, results);
+        if (waveSize > 256) throw oc::Error("waveSize must be in [1, 256], or 0 for the tuned size");
+        OcpiBatchTuning t = oc::default_tuning();
+        if (waveSize) t.waveSize = waveSize;
+        else if (count) t = oc::autotune(device, memoryBudget, jobs, count, 0, nullptr);
+        oc::run_batch_waves(device, t, memoryBudget, jobs, count, results, nullptr);
+        for (uint32_t i = 0; i < count; ++i)
+            if (results[i].status != 0) throw oc::Error("some builds of the batch failed (see their results)");
+    });
+}
+
+int ocpi_batch_autotune(int device, uint64_t memoryBudget, const OcpiJob* jobs, uint32_t count, uint32_t sampleJobs,
+                        const char* cachePath, OcpiBatchTuning* tuning) {
+    return oc::guarded([&] {
+        if (!jobs || !tuning) throw oc::Error("null argument");
+        *tuning = oc::autotune(device, memoryBudget, jobs, count, sampleJobs, cachePath);
+    });
+}
+
+int ocpi_batch_build_tuned(int device, uint64_t memoryBudget, OcpiBatchTuning* tuning, const OcpiJob* jobs,
+                           uint32_t count, OcpiJobResult* results) {
+    return oc::guarded([&] {
+        if (!jobs || !results || !tuning) throw oc::Error("null argument");
+        oc::validate_tuning(*tuning);
+        int issue = -1;
+        oc::run_batch_waves(device, *tuning, memoryBudget, jobs, count, results, &issue);
+        tuning->lastIssue = issue == 1 ? 1u : 0u;
         for (uint32_t i = 0; i < count; ++i)
             if (results[i].status != 0) throw oc::Error("some builds of the batch failed (see their results)");
     });

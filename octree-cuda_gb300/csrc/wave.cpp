@@ -38,6 +38,7 @@ Wave::Wave(int device, int num_sms) : device_(device), sms_(std::max(num_sms, 1)
 
 Wave::~Wave() {
     if (stream_) cudaStreamSynchronize(stream_);
+    if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
     if (done_event_) cudaEventDestroy(done_event_);
     if (stage_free_) cudaEventDestroy(stage_free_);
     if (stream_) cudaStreamDestroy(stream_);
@@ -226,7 +227,7 @@ void Wave::issue_steps(const std::vector<Step>& steps, const std::vector<std::pa
             }
             if (!st.n_nodes) continue;
             check_cuda(cudaMemsetAsync(work_.p, 0, 4, stream_), "memset");
-            launch_subsample_wave(st.args, st.wn, sms_, st.balance, stream_);
+            launch_subsample_wave(st.args, st.wn, sms_, st.balance, stream_, caps_);
         }
     };
     if (graphs_) {

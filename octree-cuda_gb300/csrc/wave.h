@@ -54,8 +54,10 @@ public:
     // Slot `slot` submits nothing (it failed before subsampling).
     void leave(uint32_t slot);
 
-    // Capture the schedule into a CUDA graph (default) or launch it directly.
+    // Capture the schedule into a CUDA graph (default) or launch it directly;
+    // the cluster caps of its subsampling launches.
     void set_graphs(bool on) { graphs_ = on; }
+    void set_cluster_caps(const ClusterCaps& caps) { caps_ = caps; }
     // How the last wave was issued: 1 one graph launch, 0 direct launches.
     int last_issue() const { return last_issue_; }
 
@@ -71,6 +73,7 @@ private:
         uint32_t global_cap = 0;
         cudaEvent_t ready = nullptr;
         bool submitted = false;
+        bool gone = false;
     };
     struct Step {
         size_t table_off = 0;      // byte offset of the step's tables in table_
@@ -79,6 +82,7 @@ private:
         uint32_t first_plan = 0;   // the step's (slot, level) entries: refs_[first_plan, first_plan + n_plans)
         uint32_t n_plans = 0;
         SubLevelArgs args{};       // mode, record type and grid of the wave's builds
+        WaveNodes wn{};            // the step's node tables on the device
     };
     void issue();   // mutex held; every slot has submitted or left
     void issue_steps(const std::vector<Step>& steps, const std::vector<std::pair<uint32_t, uint32_t>>& refs);
@@ -86,6 +90,7 @@ private:
     int device_;
     int sms_;
     bool graphs_ = true;
+    ClusterCaps caps_{};
     int last_issue_ = -1;
     std::mutex mu_;
     std::condition_variable cv_;
@@ -99,6 +104,7 @@ private:
     DevBuf table_, work_, g_key_, g_mask_, g_base_;
     HostBuf stage_;
     cudaEvent_t stage_free_ = nullptr;
+    cudaGraphExec_t graph_exec_ = nullptr;   // the last wave's schedule
 };
 
 }   // namespace oc

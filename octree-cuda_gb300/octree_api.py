@@ -34,7 +34,7 @@ ADDED_SYMBOLS = [
     "ocpi_server_create", "ocpi_server_destroy", "ocpi_server_submit", "ocpi_server_wait",
     "ocpi_server_get_hierarchy", "ocpi_server_release", "ocpi_batch_build", "ocpi_batch_build_wave",
     "ocpi_server_cancel",
-    "ocpi_server_lane_restarts", "ocpi_debug_inject_failures",
+    "ocpi_server_lane_restarts", "ocpi_debug_inject_failures", "ocpi_batch_autotune", "ocpi_batch_build_tuned",
 ]
 
 HIER_DTYPE = np.dtype([("type", "u1"), ("mask", "u1"), ("points", "<u4"),
@@ -84,6 +84,17 @@ class OcpiJobResult(ctypes.Structure):
         ("reused", ctypes.c_uint32), ("pointsTotal", ctypes.c_uint64), ("queuedMs", ctypes.c_double), ("runMs", ctypes.c_double),
         ("totalMs", ctypes.c_double), ("deviceMs", ctypes.c_double), ("error", ctypes.c_char * 128),
     ]
+
+
+class OcpiBatchTuning(ctypes.Structure):
+    _fields_ = [
+        ("waveSize", ctypes.c_uint32), ("clusterCap", ctypes.c_uint32), ("weightedClusterCap", ctypes.c_uint32),
+        ("useGraphs", ctypes.c_uint32), ("trialMs", ctypes.c_double), ("trials", ctypes.c_uint32),
+        ("lastIssue", ctypes.c_uint32),
+    ]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
 
 
 _lib = None
@@ -143,6 +154,10 @@ def load_library(path=LIB_PATH):
         "ocpi_debug_inject_failures": [ctypes.c_int, u32],
         "ocpi_batch_build": [ctypes.c_int, u32, u64, ctypes.POINTER(OcpiJob), u32, ctypes.POINTER(OcpiJobResult)],
         "ocpi_batch_build_wave": [ctypes.c_int, u32, u64, ctypes.POINTER(OcpiJob), u32, ctypes.POINTER(OcpiJobResult)],
+        "ocpi_batch_autotune": [ctypes.c_int, u64, ctypes.POINTER(OcpiJob), u32, u32, ctypes.c_char_p,
+                                ctypes.POINTER(OcpiBatchTuning)],
+        "ocpi_batch_build_tuned": [ctypes.c_int, u64, ctypes.POINTER(OcpiBatchTuning), ctypes.POINTER(OcpiJob), u32,
+                                   ctypes.POINTER(OcpiJobResult)],
         "ocpi_estimate_memory": [u32, u32, u8, u32, u32, ctypes.c_float, u32, u32, ctypes.POINTER(u64),
                                  ctypes.POINTER(u64)],
         "ocpi_subsample_node_noalloc": [vp, u8, u32, ctypes.POINTER(d), ctypes.POINTER(d), ctypes.POINTER(d), d,
@@ -448,10 +463,34 @@ def batch_build(jobs, device=0, lanes=4, memory_budget=150 << 30):
 def batch_build_wave(jobs, device=0, wave_size=32, memory_budget=150 << 30):
     """batch_build in subsampling waves (ocpi_batch_build_wave): jobs of the
     same record type and mode, wave_size at a time, each subsampling level
-    of a wave in one launch.  Returns the OcpiJobResults."""
+    of a wave in one launch, a wave's subsampling in one CUDA graph.
+    wave_size 0: the autotuned choice.  Returns the OcpiJobResults."""
     arr = (OcpiJob * len(jobs))(*jobs)
     res = (OcpiJobResult * len(jobs))()
     rc = load_library().ocpi_batch_build_wave(device, wave_size, memory_budget, arr, len(jobs), res)
     if rc != 0 and all(r.status == 0 for r in res):
         _check(rc, "ocpi_batch_build_wave")   # rejected before any build ran
+    return list(res)
+
+
+def batch_autotune(jobs, device=0, memory_budget=150 << 30, sample_jobs=0, cache_path=None):
+    """ocpi_batch_autotune: the fastest tuning of the batched form for a batch
+    like `jobs` (measured on a sample of it, whose outputs it writes)."""
+    arr = (OcpiJob * len(jobs))(*jobs)
+    t = OcpiBatchTuning()
+    _check(load_library().ocpi_batch_autotune(device, memory_budget, arr, len(jobs), sample_jobs,
+                                              cache_path.encode() if cache_path else None, ctypes.byref(t)),
+           "ocpi_batch_autotune")
+    return t
+
+
+def batch_build_tuned(jobs, tuning, device=0, memory_budget=150 << 30):
+    """ocpi_batch_build_tuned: the batched form with an explicit tuning
+    (tuning.lastIssue tells whether the last wave ran as one graph launch).
+    Returns the OcpiJobResults."""
+    arr = (OcpiJob * len(jobs))(*jobs)
+    res = (OcpiJobResult * len(jobs))()
+    rc = load_library().ocpi_batch_build_tuned(device, memory_budget, ctypes.byref(tuning), arr, len(jobs), res)
+    if rc != 0 and all(r.status == 0 for r in res):
+        _check(rc, "ocpi_batch_build_tuned")
     return list(res)

@@ -81,6 +81,45 @@ def test_wave_batch_equals_builds_alone():
         check_same(w, r, *b)
 
 
+@pytest.mark.parametrize("graphs", [1, 0])
+def test_tuned_waves_equal_builds_alone(graphs):
+    """An explicit tuning: waves of 6, cluster caps 2/8, each wave's
+    subsampling captured into one CUDA graph (or launched directly); the
+    last wave ran the way it was asked to, and every result equals its build
+    alone."""
+    cases = mixed_cases(13)
+    want = [alone(c, g, m) for c, g, m in cases]
+    bufs = [buffers(w) for w in want]
+    jobs = [job_for(c, g, m, *b, device_bbox=(i % 5 == 0)) for i, ((c, g, m), b) in enumerate(zip(cases, bufs))]
+    tuning = octree_api.OcpiBatchTuning(waveSize=6, clusterCap=2, weightedClusterCap=8, useGraphs=graphs)
+    results = octree_api.batch_build_tuned(jobs, tuning)
+    assert tuning.lastIssue == graphs
+    for w, r, b in zip(want, results, bufs):
+        check_same(w, r, *b)
+
+
+def test_autotune_chooses_and_caches(tmp_path):
+    """ocpi_batch_autotune measures a sweep on a sample of the batch and
+    returns a valid choice; the choice is kept for the batch's signature (a
+    second call measures nothing) and written to the cache file, and a batch
+    built with wave size 0 uses it and equals its builds alone."""
+    cases = mixed_cases(10)
+    want = [alone(c, g, m) for c, g, m in cases]
+    bufs = [buffers(w) for w in want]
+    jobs = [job_for(c, g, m, *b) for (c, g, m), b in zip(cases, bufs)]
+    cache = tmp_path / "tuning.txt"
+    t = octree_api.batch_autotune(jobs, sample_jobs=10, cache_path=str(cache))
+    assert t.trials >= 5 and t.trialMs > 0
+    assert 1 <= t.waveSize <= 10 and t.clusterCap in (2, 4, 8) and t.weightedClusterCap in (8, 16)
+    again = octree_api.batch_autotune(jobs, sample_jobs=10, cache_path=str(cache))
+    assert again.as_dict() == t.as_dict()
+    line = cache.read_text().split()
+    assert int(line[1]) == t.waveSize and int(line[4]) == t.useGraphs
+    results = octree_api.batch_build_wave(jobs, wave_size=0)
+    for w, r, b in zip(want, results, bufs):
+        check_same(w, r, *b)
+
+
 def test_wave_with_a_failing_job():
     """A job whose box leaves points below it fails in its wave; the wave's
     other builds do not wait for it and equal their builds alone."""

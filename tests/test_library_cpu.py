@@ -91,8 +91,16 @@ def test_server_and_batch_argument_errors_without_gpu():
     assert L.ocpi_batch_build_wave(0, 16, 1 << 30, None, 0, None) == -1
     assert b"null argument" in L.ocpi_last_error()
     jobs, res = (octree_api.OcpiJob * 1)(), (octree_api.OcpiJobResult * 1)()
-    assert L.ocpi_batch_build_wave(0, 0, 1 << 30, jobs, 1, res) == -1
+    assert L.ocpi_batch_build_wave(0, 300, 1 << 30, jobs, 1, res) == -1
     assert b"waveSize" in L.ocpi_last_error()
+    assert L.ocpi_batch_autotune(0, 1 << 30, None, 0, 0, None, None) == -1
+    assert b"null argument" in L.ocpi_last_error()
+    tuning = octree_api.OcpiBatchTuning(waveSize=16, clusterCap=3, weightedClusterCap=16, useGraphs=1)
+    assert L.ocpi_batch_build_tuned(0, 1 << 30, ctypes.byref(tuning), jobs, 1, res) == -1
+    assert b"clusterCap" in L.ocpi_last_error()
+    tuning.clusterCap, tuning.weightedClusterCap = 4, 32
+    assert L.ocpi_batch_build_tuned(0, 1 << 30, ctypes.byref(tuning), jobs, 1, res) == -1
+    assert b"weightedClusterCap" in L.ocpi_last_error()
     t = ctypes.c_uint64()
     assert L.ocpi_server_submit(None, ctypes.byref(octree_api.OcpiJob()), ctypes.byref(t)) == -1
     assert L.ocpi_server_wait(None, 1, None) == -1
