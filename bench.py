@@ -749,7 +749,9 @@ def main():
         if i:
             init_times.append(t1 - t0)
             e2e_times.append(time.perf_counter() - t0)
-    e2e_s = statistics.mean(e2e_times)
+    # the median: the host link is shared with the machine's other GPUs, and
+    # a step now and then waits on it (every step is listed in the line)
+    e2e_s = statistics.median(e2e_times)
     e2e_s = replica_max(e2e_s, pg)
     link = link_probe(device)
     # ocpi_init_octree inside the end-to-end steps: the chunked upload, with
@@ -796,7 +798,7 @@ def main():
                   "device_ms_per_step": round(statistics.mean(gen_ms), 3), "upload_ms": upload_ms},
         "e2e": {"value": round(n * ws / e2e_s / 1e6, 3), "unit": "Mpts/s", "h2d_bytes_per_step": n * STRIDE,
                 "d2h_bytes_per_step": hier_bytes + rec_bytes, "ms": round(e2e_s * 1e3, 2),
-                "ms_median": round(statistics.median(e2e_times) * 1e3, 2), "steps": len(e2e_times),
+                "ms_mean": round(statistics.mean(e2e_times) * 1e3, 2), "steps": len(e2e_times),
                 "step_ms": [round(x * 1e3, 2) for x in e2e_times],
                 "init_ms": [round(x * 1e3, 2) for x in init_times], **link},
         "clocks": clk,

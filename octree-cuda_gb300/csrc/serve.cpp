@@ -633,21 +633,23 @@ Executor* to_executor(void* p) {
 //
 // Jobs are grouped by record type and subsampling mode (each wave runs one
 // k_subsample instantiation) and, in submission order within a group, built
-// up to `slots` at a time.  Each job of a wave runs on the slot's pooled
-// builder and host thread; their subsampling levels meet in the Wave, one
-// launch per level over all of them.  A wave admits jobs while the slots'
-// envelopes (buffers only grow) stay within the budget; a slot whose
-// envelope keeps a job out frees its builder first.
-// One pool per device, kept for the process like the batch executors: a
-// batch's builders and the wave's buffers stay allocated for the next batch.
-// Between batches the pool holds its slots' builders (their envelopes, in
-// `env`) and the wave's buffers; admission counts both.  A batch with fewer
-// slots than the pool frees the builders of the slots it does not use.
+// up to `slots` at a time.  Each job of a wave runs on a pooled builder and
+// a host thread of its own; their subsampling plans meet in the wave, which
+// issues them as one schedule (one launch per level over all of them).
+//
+// Two waves are in flight: the pool holds two sets of `slots` builders and
+// two Wave objects, and wave k uses set k mod 2.  While wave k's schedule
+// subsamples, wave k + 1's builds upload, count and distribute; wave k + 2
+// starts once wave k's builds have returned.  A wave admits jobs while the
+// envelopes of all builders (the other set's, in use, included; buffers only
+// grow) and both waves' buffers fit the budget; idle builders of its own set
+// are freed to make room.
 struct WavePool {
     std::mutex run;   // one batch at a time per pool
-    std::unique_ptr<Wave> wave;
-    std::vector<std::unique_ptr<Builder>> builders;
-    std::vector<MemoryTerms> env;
+    std::unique_ptr<Wave> wave[2];
+    std::vector<std::unique_ptr<Builder>> builders;   // set k: [k * slots, (k + 1) * slots)
+    std::vector<MemoryTerms> env;                     // read and written by the batch's own thread only
+    std::vector<uint8_t> dropped;                     // a job's thread dropped the builder (failure)
 };
 
 WavePool& wave_pool(int device) {
@@ -656,20 +658,21 @@ WavePool& wave_pool(int device) {
     std::lock_guard<std::mutex> g(mu);
     WavePool*& p = cache[device];
     if (!p) {
-        p = new WavePool;
+        p = new WavePool;   // kept for the process, like the batch executors
         int sms = 0;
         check_cuda(cudaSetDevice(device), "cudaSetDevice");
         check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "device attribute");
-        p->wave = std::make_unique<Wave>(device, sms);
+        p->wave[0] = std::make_unique<Wave>(device, sms);
+        p->wave[1] = std::make_unique<Wave>(device, sms);
     }
     return *p;
 }
 
-// One job on slot s of the running wave (on its own thread).
-OcpiJobResult run_wave_slot(int device, WavePool& pool, uint32_t s, const OcpiJob& job) {
+// One job on builder `q` of the pool, slot `s` of `wave` (on its own thread).
+OcpiJobResult run_wave_slot(int device, WavePool& pool, Wave& wave, uint32_t q, uint32_t s, const OcpiJob& job) {
     const auto t0 = Clock::now();
     OcpiJobResult r{};
-    std::unique_ptr<Builder>& b = pool.builders[s];
+    std::unique_ptr<Builder>& b = pool.builders[q];
     try {
         check_cuda(cudaSetDevice(device), "cudaSetDevice");
         const BuildConfig cfg = config_of(job);
@@ -680,7 +683,7 @@ OcpiJobResult run_wave_slot(int device, WavePool& pool, uint32_t s, const OcpiJo
             b->compute_bbox(real, cubic);
         }
         if (job.outRecords) b->set_output_host(job.outRecords, job.outLut, job.outCapacity);
-        b->join_wave(pool.wave.get(), s);
+        b->join_wave(&wave, s);
         b->generate();
         b->join_wave(nullptr, 0);
         const std::vector<uint8_t> hier = b->hierarchy();
@@ -698,10 +701,10 @@ OcpiJobResult run_wave_slot(int device, WavePool& pool, uint32_t s, const OcpiJo
         r.status = -1;
         std::snprintf(r.error, sizeof r.error, "%s", e.what());
         b.reset();   // leave no half-finished device state behind
-        pool.env[s] = MemoryTerms{};
+        pool.dropped[q] = 1;
         cudaGetLastError();
     }
-    pool.wave->leave(s);   // the other builds of the wave stop waiting for this one
+    wave.leave(s);   // the other builds of the wave stop waiting for this one
     if (b) b->join_wave(nullptr, 0);
     r.lane = s;
     r.runMs = r.totalMs = ms_between(t0, Clock::now());
@@ -714,14 +717,15 @@ void run_batch_waves(int device, const OcpiBatchTuning& tuning, uint64_t budget,
     WavePool& pool = wave_pool(device);
     std::lock_guard<std::mutex> run(pool.run);
     check_cuda(cudaSetDevice(device), "cudaSetDevice");
-    pool.wave->set_graphs(tuning.useGraphs != 0);
-    pool.wave->set_cluster_caps(ClusterCaps{tuning.clusterCap, tuning.weightedClusterCap});
-    if (pool.builders.size() > slots) {
-        pool.builders.resize(slots);   // frees the builders of the slots this batch does not use
-        pool.env.resize(slots);
+    for (auto& w : pool.wave) {
+        w->set_graphs(tuning.useGraphs != 0);
+        w->set_cluster_caps(ClusterCaps{tuning.clusterCap, tuning.weightedClusterCap});
     }
-    pool.builders.resize(slots);
-    pool.env.resize(slots, MemoryTerms{});
+    // two sets of `slots` builders; a batch with other wave sizes keeps the
+    // builders that fall on its slots and frees the rest
+    pool.builders.resize(2 * (size_t)slots);
+    pool.env.resize(2 * (size_t)slots, MemoryTerms{});
+    pool.dropped.assign(2 * (size_t)slots, 0);
     int sms = 0;
     check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "device attribute");
     std::vector<BuildConfig> cfg(count);
@@ -745,67 +749,110 @@ void run_batch_waves(int device, const OcpiBatchTuning& tuning, uint64_t budget,
         const bool inter = !c.intra && c.inter;
         groups[std::make_tuple(c.cloud_type, c.intra, inter, inter && c.weighting, c.random)].push_back(i);
     }
-    for (auto& kv : groups) {
-        const std::vector<uint32_t>& ids = kv.second;
-        for (size_t next = 0; next < ids.size();) {
-            // the next wave: jobs in order while every slot's envelope (the
-            // idle slots' too: their builders keep their buffers) fits
-            std::vector<uint32_t> wave;
-            // the wave's own buffers: what it holds, or what this wave's
-            // largest possible jobs need, whichever is more
+    std::vector<uint32_t> order;   // jobs group by group, in submission order within a group
+    for (auto& kv : groups) order.insert(order.end(), kv.second.begin(), kv.second.end());
+
+    struct Running {
+        std::vector<uint32_t> jobs;
+        std::vector<std::thread> threads;
+    };
+    Running running[2];
+    auto finish = [&](int set) {
+        for (auto& t : running[set].threads) t.join();
+        running[set].threads.clear();
+        running[set].jobs.clear();
+        for (size_t q = (size_t)set * slots; q < (size_t)set * slots + slots; ++q)
+            if (pool.dropped[q]) {
+                pool.env[q] = MemoryTerms{};
+                pool.dropped[q] = 0;
+            }
+    };
+    try {
+        size_t next = 0;
+        for (uint64_t k = 0; next < order.size(); ++k) {
+            const int set = (int)(k & 1);
+            finish(set);   // wave k - 2: this set's builders and wave are idle again
+            Wave& wave = *pool.wave[set];
+            const size_t base = (size_t)set * slots;
+            // the wave: consecutive jobs of one group
+            const auto group_of = [&](uint32_t i) {
+                const BuildConfig& c = cfg[i];
+                const bool inter = !c.intra && c.inter;
+                return std::make_tuple(c.cloud_type, c.intra, inter, inter && c.weighting, c.random);
+            };
             uint64_t wave_nodes = 0;
             uint32_t wave_gcap = 0;
-            for (size_t q = next, k = 0; q < ids.size() && k < slots; ++q, ++k) {
-                wave_nodes += terms[ids[q]].node_cap;
-                wave_gcap = std::max<uint32_t>(wave_gcap, (uint32_t)terms[ids[q]].slots);
+            for (size_t q = next, n = 0; q < order.size() && n < slots && group_of(order[q]) == group_of(order[next]);
+                 ++q, ++n) {
+                wave_nodes += terms[order[q]].node_cap;
+                wave_gcap = std::max<uint32_t>(wave_gcap, (uint32_t)terms[order[q]].slots);
             }
-            const uint64_t wave_bytes =
-                std::max(pool.wave->device_bytes(), Wave::bytes_for(sms, slots, wave_nodes, wave_gcap));
-            uint64_t used = wave_bytes;
+            uint64_t used = std::max(wave.device_bytes(), Wave::bytes_for(sms, slots, wave_nodes, wave_gcap)) +
+                            pool.wave[set ^ 1]->device_bytes();
             for (const MemoryTerms& e : pool.env) used += device_bytes(e);
             auto free_slot = [&](size_t q) {
                 used = used - device_bytes(pool.env[q]) + device_bytes(MemoryTerms{});
                 pool.env[q] = MemoryTerms{};
                 pool.builders[q].reset();
             };
-            for (size_t s = 0; s < slots && next < ids.size(); ++s) {
-                const uint32_t i = ids[next];
-                MemoryTerms env = envelope(pool.env[s], terms[i]);
-                if (used - device_bytes(pool.env[s]) + device_bytes(env) > budget) {
-                    // this slot's buffers, then those of the idle slots after
-                    // it, make room; the slots before it hold this wave's jobs
-                    free_slot(s);
+            std::vector<uint32_t>& wj = running[set].jobs;
+            for (size_t s = 0; s < slots && next < order.size(); ++s) {
+                const uint32_t i = order[next];
+                if (!wj.empty() && group_of(i) != group_of(wj[0])) break;   // one group per wave
+                const size_t q = base + s;
+                MemoryTerms env = envelope(pool.env[q], terms[i]);
+                if (used - device_bytes(pool.env[q]) + device_bytes(env) > budget) {
+                    // this builder's buffers, then those of the idle builders
+                    // after it in this set, make room; the builders before it
+                    // hold this wave's jobs and the other set's the running wave's
+                    free_slot(q);
                     env = terms[i];
-                    auto fits = [&] { return used - device_bytes(pool.env[s]) + device_bytes(env) <= budget; };
-                    for (size_t q = slots; q-- > s + 1 && !fits();) free_slot(q);
+                    auto fits = [&] { return used - device_bytes(pool.env[q]) + device_bytes(env) <= budget; };
+                    for (size_t r = base + slots; r-- > q + 1 && !fits();) free_slot(r);
                     if (!fits()) break;
                 }
-                used += device_bytes(env) - device_bytes(pool.env[s]);
-                pool.env[s] = env;
-                wave.push_back(i);
+                used += device_bytes(env) - device_bytes(pool.env[q]);
+                pool.env[q] = env;
+                wj.push_back(i);
                 ++next;
             }
-            if (wave.empty()) throw Error("no job of the batch fits the budget beside the pooled builders");
+            if (wj.empty()) {
+                // nothing fits beside the other wave: let it finish, then retry
+                // with this set alone holding memory
+                if (!running[set ^ 1].jobs.empty()) {
+                    finish(set ^ 1);
+                    for (size_t q = (size_t)(set ^ 1) * slots; q < (size_t)(set ^ 1) * slots + slots; ++q)
+                        free_slot(q);
+                    --k;   // the same set again
+                    continue;
+                }
+                throw Error("no job of the batch fits the budget beside the pooled builders");
+            }
             std::vector<uint32_t> depths;
-            for (uint32_t i : wave) {
+            uint64_t max_nodes = 0;
+            uint32_t max_gcap = 0;
+            for (uint32_t i : wj) {
                 uint32_t d = 0;   // tree depth: log2 of the (validated, power-of-two) chunking grid
                 while ((1u << d) < cfg[i].chunk_grid) ++d;
                 depths.push_back(d);
-            }
-            uint64_t max_nodes = 0;
-            uint32_t max_gcap = 0;
-            for (uint32_t i : wave) {
                 max_nodes += terms[i].node_cap;
                 max_gcap = std::max<uint32_t>(max_gcap, (uint32_t)terms[i].slots);
             }
-            pool.wave->start(depths, max_nodes, max_gcap);
-            std::vector<std::thread> threads;
-            for (uint32_t s = 0; s < wave.size(); ++s)
-                threads.emplace_back([&, s] { results[wave[s]] = run_wave_slot(device, pool, s, jobs[wave[s]]); });
-            for (auto& t : threads) t.join();
-            if (last_issue) *last_issue = pool.wave->last_issue();
+            wave.start(depths, max_nodes, max_gcap);
+            for (uint32_t s = 0; s < wj.size(); ++s)
+                running[set].threads.emplace_back([&, set, s, base] {
+                    results[running[set].jobs[s]] =
+                        run_wave_slot(device, pool, *pool.wave[set], (uint32_t)(base + s), s, jobs[running[set].jobs[s]]);
+                });
         }
+    } catch (...) {
+        finish(0);
+        finish(1);
+        throw;
     }
+    finish(0);
+    finish(1);
+    if (last_issue) *last_issue = std::max(pool.wave[0]->last_issue(), pool.wave[1]->last_issue());
 }
 
 // ---- autotuning of the batched form
