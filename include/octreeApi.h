@@ -276,7 +276,7 @@ OCPI_EXPORT int ocpi_batch_build_tuned(int device, uint64_t memoryBudget, OcpiBa
  * Limits and sharing:
  *   - at most OCPI_NOALLOC_MAX_CANDIDATES candidate points per call; larger
  *     nodes are rejected with -1 and a message in ocpi_last_error();
- *   - the scratch (OCPI_NOALLOC_SCRATCH_BYTES, 16.5 MiB) is held on every GPU
+ *   - the scratch (OCPI_NOALLOC_SCRATCH_BYTES, 12.5 MiB) is held on every GPU
  *     where this library's subsampling module is loaded, until process exit;
  *   - every call shares the scratch and it keeps the last call's contents;
  *     calls that overlap on the GPU (other streams, other host threads) race
@@ -304,7 +304,7 @@ OCPI_EXPORT int ocpi_batch_build_tuned(int device, uint64_t memoryBudget, OcpiBa
  *                     (1 point below the node box, 4 brick table overflow)
  */
 #define OCPI_NOALLOC_MAX_CANDIDATES (131072u)
-#define OCPI_NOALLOC_SCRATCH_BYTES (17302784u)
+#define OCPI_NOALLOC_SCRATCH_BYTES (13108480u)
 #define OCPI_SUB_INTRA (1u)
 #define OCPI_SUB_INTER (2u)
 #define OCPI_SUB_RANDOM (8u)

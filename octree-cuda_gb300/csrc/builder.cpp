@@ -571,7 +571,7 @@ uint64_t device_bytes(const MemoryTerms& t) {
     uint64_t per_cand = 4 + 8 + 4;       // key cache, selection key, cell list
     if (t.random) per_cand += 4;         // selected candidate
     if (t.packed) per_cand += 8;         // packed colour sums
-    if (t.weighted) per_cand += 12 + 4 + 4 + 20 + 32;   // cell units, cell groups, weighted sums
+    if (t.weighted) per_cand += 12 + 4 + 4 + 20;   // cell units, cell groups
     uint64_t b = 0;
     b += t.cloud_bytes + 64;                                           // cloud
     b += t.cells * 4;                                                  // count pyramid
@@ -1111,7 +1111,6 @@ void Builder::subsample() {
             csr_count_.ensure(scratch_cap * 4);
             csr_start_.ensure(scratch_cap * 4);
             csr_pts_.ensure(scratch_cap * 20);
-            acc_w_.ensure(scratch_cap * 32);
         }
         stage_lut_.ensure(stage_cap * 4);
         stage_rec_.ensure(stage_cap * 18 + 64);
@@ -1160,7 +1159,6 @@ void Builder::subsample() {
         a.csr_count = csr_count_.as<uint32_t>();
         a.csr_start = csr_start_.as<uint32_t>();
         a.csr_pts = csr_pts_.as<uint8_t>();
-        a.acc_w = acc_w_.as<uint64_t>();
         a.out = op;
         a.work_counter = work_.as<uint32_t>();
         a.err = err_.as<uint32_t>();

@@ -296,17 +296,14 @@ __device__ __forceinline__ uint64_t inter_sum(const BrickMap& bm, uint32_t slot,
     return e;
 }
 
-// Distance weighting, source side: the candidates of one occupied cell (its
-// CSR list [s0, s1)) add their weighted colours to every occupied cell of its
-// 3x3x3 neighbourhood, itself included, with one 64-bit reduction per sum and
-// target cell.  Integer sums make the result independent of the order in
-// which the reductions land.
-struct WeightedScatter {
-    const uint8_t* pts;          // the node's CSR entries (cell units x, y, z; r | g << 16; b)
-    uint32_t s0, s1;
-    unsigned long long* acc;     // the node's cells: 4 sums (r, g, b, weight) each
-    __device__ __forceinline__ void operator()(uint32_t n, int x, int y, int z) {
-        uint64_t sr = 0, sg = 0, sb = 0, sw = 0;
+struct WeightedSum {
+    const uint32_t* start;
+    const uint32_t* count;
+    const uint8_t* pts;
+    int x, y, z;
+    uint64_t sr, sg, sb, sw;
+    __device__ __forceinline__ void operator()(uint32_t n, int, int, int) {
+        const uint32_t s0 = start[n], s1 = s0 + count[n];
         for (uint32_t p = s0; p < s1; ++p) {
             const uint32_t* q = reinterpret_cast<const uint32_t*>(pts + (uint64_t)p * 20);
             const uint32_t wq = weight_q(__uint_as_float(q[0]), __uint_as_float(q[1]), __uint_as_float(q[2]), x, y, z);
@@ -315,10 +312,6 @@ struct WeightedScatter {
             sb += (uint64_t)wq * (q[4] & 0xFFFF);
             sw += wq;
         }
-        atomicAdd(acc + 4 * (uint64_t)n + 0, (unsigned long long)sr);
-        atomicAdd(acc + 4 * (uint64_t)n + 1, (unsigned long long)sg);
-        atomicAdd(acc + 4 * (uint64_t)n + 2, (unsigned long long)sb);
-        atomicAdd(acc + 4 * (uint64_t)n + 3, (unsigned long long)sw);
     }
 };
 
@@ -605,11 +598,7 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a0, W
         for (uint32_t r = tid0; r < cells; r += tstride) {
             a.acc_best[off + r] = ~0ull;
             if (averaged && !weighted) a.acc_intra[off + r] = 0;
-            if (weighted) {
-                a.csr_count[off + r] = 0;
-                reinterpret_cast<uint4*>(a.acc_w + (off + r) * 4)[0] = make_uint4(0, 0, 0, 0);
-                reinterpret_cast<uint4*>(a.acc_w + (off + r) * 4)[1] = make_uint4(0, 0, 0, 0);
-            }
+            if (weighted) a.csr_count[off + r] = 0;
         }
         sync_all();
 
@@ -722,21 +711,6 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a0, W
                 }
             }
             sync_all();
-            // every occupied cell adds its candidates' weighted colours to its
-            // occupied neighbours (kernel_inter_cell_filtering.cuh:109-194 with
-            // fixed-point weights)
-            for (uint32_t r = tid0; r < cells; r += tstride) {
-                const uint32_t ks = a.cell_slot[off + r];
-                const uint32_t slot = ks >> 6, bit = ks & 63;
-                const uint32_t brick = bm.key[slot] - 1;
-                const int bx = (int)(brick & 0xFF), by = (int)((brick >> 8) & 0xFF), bz = (int)(brick >> 16);
-                const int lx = (int)(bit & 3), ly = (int)((bit >> 2) & 3), lz = (int)((bit >> 4) & 3);
-                const uint32_t s0 = a.csr_start[off + r];
-                WeightedScatter f{a.csr_pts + off * 20, s0, s0 + a.csr_count[off + r],
-                                  reinterpret_cast<unsigned long long*>(a.acc_w + off * 4)};
-                visit_neighbours(bm, slot, bx, by, bz, lx, ly, lz, f);
-            }
-            sync_all();
         }
 
         // ---- emit one record per occupied cell (thread per cell, rank order;
@@ -775,14 +749,13 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a0, W
                 } else if (inter && !weighted) {
                     decode_colors(inter_sum(bm, slot, bx, by, bz, lx, ly, lz, a.acc_intra + off), cr, cg, cb);
                 } else if (weighted) {
-                    const uint4* w4 = reinterpret_cast<const uint4*>(a.acc_w + (off + r) * 4);
-                    const uint4 lo = __ldcg(w4), hi = __ldcg(w4 + 1);   // sums written by reductions (L2)
-                    const uint64_t sr = ((uint64_t)lo.y << 32) | lo.x, sg = ((uint64_t)lo.w << 32) | lo.z;
-                    const uint64_t sb = ((uint64_t)hi.y << 32) | hi.x, sw = ((uint64_t)hi.w << 32) | hi.z;
-                    if (sw) {
-                        cr = (uint16_t)(sr / sw);
-                        cg = (uint16_t)(sg / sw);
-                        cb = (uint16_t)(sb / sw);
+                    WeightedSum f{a.csr_start + off, a.csr_count + off, a.csr_pts + off * 20,
+                                  bx * 4 + lx, by * 4 + ly, bz * 4 + lz, 0, 0, 0, 0};
+                    visit_neighbours(bm, slot, bx, by, bz, lx, ly, lz, f);
+                    if (f.sw) {
+                        cr = (uint16_t)(f.sr / f.sw);
+                        cg = (uint16_t)(f.sg / f.sw);
+                        cb = (uint16_t)(f.sb / f.sw);
                     }
                 }
                 a.out_lut[oo + r] = idx;

@@ -108,7 +108,7 @@ struct SubLevelArgs {
     uint32_t* cell_slot;        // per cell: brick slot holding it
     uint64_t* acc_intra;        // per cell: packed colour sum
     uint64_t* acc_inter;        // per cell: packed colour sum over the 3x3x3 neighbourhood
-    uint64_t* acc_w;            // per cell: 4 x fixed-point weighted sums r, g, b, weight (weighted only; 32-byte aligned)
+    uint64_t* acc_w;            // per cell: 4 x fixed-point weighted sums (weighted only)
     uint32_t* csr_count;        // per cell: candidates in the cell (weighted only)
     uint32_t* csr_start;        // per cell
     uint8_t* csr_pts;           // per candidate: grouped by cell (weighted only), 20 bytes each

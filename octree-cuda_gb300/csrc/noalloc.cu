@@ -10,7 +10,7 @@
 // works in a fixed scratch array that is part of the library image.
 //
 // The scratch is a file-scope __device__ array of kScratchBytes (about
-// 16.5 MiB).  Every GPU on which this library's module is loaded holds it
+// 12.5 MiB).  Every GPU on which this library's module is loaded holds it
 // until the process exits.  Every call shares it, and it keeps whatever the
 // last call left: the set-up kernel below clears the words that must start at
 // zero, and the subsample kernel clears its own per-node state.  Two calls
@@ -60,8 +60,7 @@ constexpr size_t kOffIntra = align256(kOffSlot + 4ull * kMaxCandidates);     // 
 constexpr size_t kOffCsrCount = align256(kOffIntra + 8ull * kMaxCandidates); // u32 per cell
 constexpr size_t kOffCsrStart = align256(kOffCsrCount + 4ull * kMaxCandidates);
 constexpr size_t kOffCsrPts = align256(kOffCsrStart + 4ull * kMaxCandidates);  // 20 B per candidate
-constexpr size_t kOffAccW = align256(kOffCsrPts + 20ull * kMaxCandidates);     // 4 x u64 per cell
-constexpr size_t kOffGKey = align256(kOffAccW + 32ull * kMaxCandidates);       // u32 per brick slot
+constexpr size_t kOffGKey = align256(kOffCsrPts + 20ull * kMaxCandidates);     // u32 per brick slot
 constexpr size_t kOffGMask = align256(kOffGKey + 4ull * kMaxBrickSlots);       // u64 per brick slot
 constexpr size_t kOffGBase = align256(kOffGMask + 8ull * kMaxBrickSlots);      // u32 per brick slot
 constexpr size_t kScratchBytes = align256(kOffGBase + 4ull * kMaxBrickSlots);
@@ -187,7 +186,6 @@ extern "C" int ocpi_subsample_node_noalloc(const uint8_t* cloud, uint8_t cloudTy
         a.csr_count = reinterpret_cast<uint32_t*>(base + kOffCsrCount);
         a.csr_start = reinterpret_cast<uint32_t*>(base + kOffCsrStart);
         a.csr_pts = base + kOffCsrPts;
-        a.acc_w = reinterpret_cast<uint64_t*>(base + kOffAccW);
         for (int k = 0; k < 3; ++k) a.out.ax[k] = make_out_axis(cloudMin[k], 1.0 / scale[k]);
         a.work_counter = work;
         a.err = outStatus + 1;
