@@ -238,7 +238,7 @@ OCPI_EXPORT int ocpi_batch_build(int device, uint32_t lanes, uint64_t memoryBudg
 OCPI_EXPORT int ocpi_batch_build_wave(int device, uint32_t waveSize, uint64_t memoryBudget, const OcpiJob* jobs,
                                       uint32_t count, OcpiJobResult* results);
 
-/* Tuning of the batched form in waves. */
+/* Tuning of the batched form: subsampling waves, or the lane executor. */
 typedef struct OcpiBatchTuning {
     uint32_t waveSize;            /* builds per wave, 1..256 */
     uint32_t clusterCap;          /* largest thread-block cluster per node of a subsampling level: 1, 2, 4 or 8 */
@@ -247,19 +247,22 @@ typedef struct OcpiBatchTuning {
     double trialMs;               /* ocpi_batch_autotune: measured time of this choice on its sample */
     uint32_t trials;              /* ocpi_batch_autotune: configurations measured */
     uint32_t lastIssue;           /* set by the library: 1 if the last wave ran as one graph launch */
+    uint32_t lanes;               /* 0: waves as above; 1..64: the lane executor (ocpi_batch_build) with this
+                                     many lanes, the wave fields unused */
 } OcpiBatchTuning;
 
-/* Measures ocpi_batch_build_wave on an evenly spaced sample of the jobs (at
- * most sampleJobs of them, 0: 48; their output arrays are written) over a
- * sweep of wave sizes, cluster caps and graph capture, and returns the
- * fastest in `tuning`.  The choice is kept for the rest of the process per
+/* Measures the batched form on an evenly spaced sample of the jobs (at most
+ * sampleJobs of them, 0: 48; their output arrays are written): subsampling
+ * waves over a sweep of wave sizes, cluster caps and graph capture, and the
+ * lane executor with 4 lanes; returns the fastest in `tuning`.  The choice is kept for the rest of the process per
  * device and batch signature (job count, mean size, share of float64 clouds,
  * of distance-weighted jobs and of 512-grid jobs, each in buckets); with a
  * cachePath it is also read from and appended to that text file, so that a
  * later process starts tuned. */
 OCPI_EXPORT int ocpi_batch_autotune(int device, uint64_t memoryBudget, const OcpiJob* jobs, uint32_t count,
                                     uint32_t sampleJobs, const char* cachePath, OcpiBatchTuning* tuning);
-/* ocpi_batch_build_wave with an explicit tuning; tuning->lastIssue is set */
+/* the batched form with an explicit tuning (waves, or lanes when
+   tuning->lanes > 0); tuning->lastIssue is set */
 OCPI_EXPORT int ocpi_batch_build_tuned(int device, uint64_t memoryBudget, OcpiBatchTuning* tuning,
                                        const OcpiJob* jobs, uint32_t count, OcpiJobResult* results);
 

@@ -636,9 +636,13 @@ void Builder::upload(const uint8_t* host_cloud, bool wait, bool count) {
     tree_valid_ = false;
     reuse_tree_ = false;
     counted_ = false;
-    constexpr uint32_t kChunks = 16;
+    // up to 16 chunks of at least 64 MB: a large cloud's counting overlaps
+    // its upload, a small cloud's upload is one copy and one counting launch
     constexpr uint64_t kChunkAlign = 1024;   // chunk starts: a multiple of the counting tile (16-byte aligned)
-    if (count && cfg_.has_bbox() && cfg_.n >= 4 * kChunks * kChunkAlign) {
+    constexpr uint64_t kMinChunkBytes = 64ull << 20;
+    const uint32_t kChunks =
+        (uint32_t)std::min<uint64_t>(16, std::max<uint64_t>(1, (uint64_t)cfg_.n * cfg_.stride / kMinChunkBytes));
+    if (count && cfg_.has_bbox() && cfg_.n >= 4 * kChunkAlign) {
         const bool sparse = sparse_cloud();
         while (chunk_ready_.size() < kChunks) {
             cudaEvent_t e;
@@ -967,6 +971,7 @@ void Builder::subsample() {
     std::vector<uint32_t> level_first(depth_ + 2, 0), ii_of(n, 0xFFFFFFFFu);
     std::vector<uint32_t> order;
     std::vector<uint32_t> balance(depth_ + 2, 1);   // see launch_subsample_level
+    std::vector<uint32_t> node_blocks(depth_ + 2, 1);
     uint64_t max_level_bound = 0, max_node_bound = 0;
     for (uint32_t l = 1; l <= depth_; ++l) {
         auto list = internal_by_level_[l];
@@ -982,6 +987,7 @@ void Builder::subsample() {
         }
         max_level_bound = std::max(max_level_bound, lb);
         if (lb) balance[l] = (uint32_t)std::min<uint64_t>(64, (in_bound[list[0]] * num_sms_ + lb - 1) / lb);
+        if (!list.empty()) node_blocks[l] = node_blocks_for(in_bound[list[0]]);
     }
     level_first[depth_ + 1] = (uint32_t)order.size();
     const uint32_t n_internal = (uint32_t)order.size();
@@ -1209,7 +1215,9 @@ void Builder::subsample() {
                 a.nodes = lvl;
                 a.n_nodes = cnt;
                 a.out_points = out_points_.as<uint32_t>() + first;
-                launches_ += launch_subsample_level(a, num_sms_, balance[l], stream_);
+                ClusterCaps caps;
+                caps.node_blocks = node_blocks[l];
+                launches_ += launch_subsample_level(a, num_sms_, balance[l], stream_, caps);
                 char mark[32];
                 std::snprintf(mark, sizeof mark, "sub_l%u", l);
                 stage_mark(mark);

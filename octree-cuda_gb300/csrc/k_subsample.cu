@@ -869,7 +869,7 @@ uint32_t cluster_size(uint32_t n_nodes, int num_sms, uint32_t cap) {
 template <bool kF32, int kColor, bool kRandom, bool kWave>
 void launch_one(const SubLevelArgs& a, const WaveNodes& wn, int num_sms, uint32_t balance, size_t smem,
                 cudaStream_t stream, const ClusterCaps& caps) {
-    const uint32_t cap = kColor == 3 ? caps.weighted : caps.plain;
+    const uint32_t cap = std::min(kColor == 3 ? caps.weighted : caps.plain, std::max(caps.node_blocks, 1u));
     uint32_t cs = cluster_size(a.n_nodes, num_sms, cap);
     if (kColor == 3)
         while (cs < cap && cs < balance) cs <<= 1;
@@ -929,11 +929,11 @@ void launch_mode(const SubLevelArgs& a, const WaveNodes& wn, int num_sms, uint32
 
 }   // namespace
 
-int launch_subsample_level(const SubLevelArgs& a, int num_sms, uint32_t balance_blocks, cudaStream_t stream) {
+int launch_subsample_level(const SubLevelArgs& a, int num_sms, uint32_t balance_blocks, cudaStream_t stream,
+                           const ClusterCaps& caps) {
     if (!a.n_nodes) return 0;
     const size_t smem = subsample_smem_bytes();
     const WaveNodes none{};
-    const ClusterCaps caps{};
     if (a.float_input) launch_mode<true, false>(a, none, num_sms, balance_blocks, smem, stream, caps);
     else launch_mode<false, false>(a, none, num_sms, balance_blocks, smem, stream, caps);
     return 1;

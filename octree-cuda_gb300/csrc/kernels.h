@@ -188,23 +188,36 @@ struct WaveNodes {
     const uint32_t* local;
 };
 
+// Largest thread-block cluster per node of a subsampling level: unweighted
+// modes, and distance-weighted ones (clusters above 8 are non-portable).
+struct ClusterCaps {
+    uint32_t plain = 4;
+    uint32_t weighted = 16;
+    // the level's largest node needs no more blocks than this (one per
+    // kCandidatesPerClusterBlock of its candidates): small nodes are not
+    // split over blocks that would mostly wait at the cluster barriers
+    uint32_t node_blocks = 16;
+};
+constexpr uint64_t kCandidatesPerClusterBlock = 8192;
+// node_blocks for a level whose largest node has `max_bound` candidates
+inline uint32_t node_blocks_for(uint64_t max_bound) {
+    uint32_t b = 1;
+    while (b < 16 && (uint64_t)b * 2 * kCandidatesPerClusterBlock <= max_bound) b <<= 1;
+    return b;
+}
+
 size_t subsample_smem_bytes();
 uint32_t subsample_block_size();
 // balance_blocks: the blocks the level's largest node needs for its share
 // of the work to equal one SM's share of the whole level (largest candidate
 // bound x SMs / sum of the bounds); distance-weighted levels size their
 // clusters by it.
-int launch_subsample_level(const SubLevelArgs& a, int num_sms, uint32_t balance_blocks, cudaStream_t stream);
+int launch_subsample_level(const SubLevelArgs& a, int num_sms, uint32_t balance_blocks, cudaStream_t stream,
+                           const ClusterCaps& caps = ClusterCaps{});
 // `wave` holds what the step shares: n_nodes (all builds' nodes), the work
 // counter, the per-block global brick tables, the mode and record type; the
 // build-specific fields come from wn.clouds.  A node whose build has the
 // capacity error set is skipped.
-// Largest thread-block cluster per node of a subsampling level: unweighted
-// modes, and distance-weighted ones (clusters above 8 are non-portable).
-struct ClusterCaps {
-    uint32_t plain = 4;
-    uint32_t weighted = 16;
-};
 int launch_subsample_wave(const SubLevelArgs& wave, const WaveNodes& wn, int num_sms, uint32_t balance_blocks,
                           cudaStream_t stream, const ClusterCaps& caps = ClusterCaps{});
 

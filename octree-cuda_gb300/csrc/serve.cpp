@@ -904,6 +904,7 @@ bool load_tuning(const char* path, const std::string& sig, OcpiBatchTuning& t) {
         OcpiBatchTuning v{};
         if (in >> key >> v.waveSize >> v.clusterCap >> v.weightedClusterCap >> v.useGraphs >> v.trialMs >> v.trials &&
             key == sig) {
+            if (!(in >> v.lanes)) v.lanes = 0;
             t = v;
             found = true;
         }
@@ -915,10 +916,12 @@ void store_tuning(const char* path, const std::string& sig, const OcpiBatchTunin
     if (!path) return;
     std::ofstream f(path, std::ios::app);
     f << sig << ' ' << t.waveSize << ' ' << t.clusterCap << ' ' << t.weightedClusterCap << ' ' << t.useGraphs << ' '
-      << t.trialMs << ' ' << t.trials << '\n';
+      << t.trialMs << ' ' << t.trials << ' ' << t.lanes << '\n';
 }
 
 void validate_tuning(const OcpiBatchTuning& t) {
+    if (t.lanes > 64) throw Error("lanes must be in [0, 64]");
+    if (t.lanes) return;
     if (t.waveSize < 1 || t.waveSize > 256) throw Error("waveSize must be in [1, 256]");
     if (t.clusterCap < 1 || t.clusterCap > 8 || (t.clusterCap & (t.clusterCap - 1)))
         throw Error("clusterCap must be 1, 2, 4 or 8");
@@ -936,6 +939,38 @@ OcpiBatchTuning default_tuning() {
 }
 
 }   // namespace
+
+// The lane executor on a batch: every job checked before any starts, results
+// in order.
+void run_batch_lanes(int device, uint32_t lanes, uint64_t budget, const OcpiJob* jobs, uint32_t count,
+                     OcpiJobResult* results) {
+    if (lanes < 1 || lanes > 64) throw Error("lanes must be in [1, 64]");
+    Executor& ex = batch_executor(device, lanes, budget);
+    // a refused job leaves no other job of the batch running after the call returns
+    for (uint32_t i = 0; i < count; ++i) {
+        try {
+            ex.check(jobs[i]);
+        } catch (const std::exception& e) {
+            throw Error("job " + std::to_string(i) + " of the batch: " + e.what());
+        }
+    }
+    std::vector<uint64_t> tickets(count);
+    for (uint32_t i = 0; i < count; ++i) tickets[i] = ex.submit(jobs[i]);
+    for (uint32_t i = 0; i < count; ++i) {
+        results[i] = ex.wait(tickets[i]);
+        ex.release(tickets[i]);
+    }
+}
+
+void run_batch_tuned(int device, const OcpiBatchTuning& t, uint64_t budget, const OcpiJob* jobs, uint32_t count,
+                     OcpiJobResult* results, int* last_issue) {
+    if (t.lanes) {
+        run_batch_lanes(device, t.lanes, budget, jobs, count, results);
+        if (last_issue) *last_issue = 0;
+    } else {
+        run_batch_waves(device, t, budget, jobs, count, results, last_issue);
+    }
+}
 
 OcpiBatchTuning autotune(int device, uint64_t budget, const OcpiJob* jobs, uint32_t count, uint32_t sample_jobs,
                          const char* cache_path) {
@@ -959,7 +994,7 @@ OcpiBatchTuning autotune(int device, uint64_t budget, const OcpiJob* jobs, uint3
     uint32_t trials = 0;
     auto measure = [&](const OcpiBatchTuning& t) {
         const auto t0 = Clock::now();
-        run_batch_waves(device, t, budget, sample.data(), m, res.data(), nullptr);
+        run_batch_tuned(device, t, budget, sample.data(), m, res.data(), nullptr);
         const double ms = ms_between(t0, Clock::now());
         for (const auto& r : res)
             if (r.status != 0) throw Error(std::string("autotune trial failed: ") + r.error);
@@ -972,8 +1007,9 @@ OcpiBatchTuning autotune(int device, uint64_t budget, const OcpiJob* jobs, uint3
     best.trialMs = measure(best);
     auto consider = [&](OcpiBatchTuning t) {
         if (t.waveSize == best.waveSize && t.clusterCap == best.clusterCap &&
-            t.weightedClusterCap == best.weightedClusterCap && t.useGraphs == best.useGraphs)
+            t.weightedClusterCap == best.weightedClusterCap && t.useGraphs == best.useGraphs && t.lanes == best.lanes)
             return;
+        if (t.lanes) measure(t);   // the executor's builders grow on its first run
         t.trialMs = measure(t);
         if (t.trialMs < best.trialMs) best = t;
     };
@@ -993,6 +1029,11 @@ OcpiBatchTuning autotune(int device, uint64_t budget, const OcpiJob* jobs, uint3
     {
         OcpiBatchTuning t = best;
         t.useGraphs = 0;
+        consider(t);
+    }
+    {
+        OcpiBatchTuning t = best;   // the lane executor instead of waves
+        t.lanes = 4;
         consider(t);
     }
     best.trials = trials;
@@ -1064,26 +1105,9 @@ int ocpi_batch_build(int device, uint32_t lanes, uint64_t memoryBudget, const Oc
                      OcpiJobResult* results) {
     return oc::guarded([&] {
         if (!jobs || !results) throw oc::Error("null argument");
-        if (lanes < 1 || lanes > 64) throw oc::Error("lanes must be in [1, 64]");
-        oc::Executor& ex = oc::batch_executor(device, lanes, memoryBudget);
-        // every job is checked before any starts: a refused job leaves no
-        // other job of the batch running after the call returns
-        for (uint32_t i = 0; i < count; ++i) {
-            try {
-                ex.check(jobs[i]);
-            } catch (const std::exception& e) {
-                throw oc::Error("job " + std::to_string(i) + " of the batch: " + e.what());
-            }
-        }
-        std::vector<uint64_t> tickets(count);
-        for (uint32_t i = 0; i < count; ++i) tickets[i] = ex.submit(jobs[i]);
-        bool ok = true;
-        for (uint32_t i = 0; i < count; ++i) {
-            results[i] = ex.wait(tickets[i]);
-            ex.release(tickets[i]);
-            ok = ok && results[i].status == 0;
-        }
-        if (!ok) throw oc::Error("some builds of the batch failed (see their results)");
+        oc::run_batch_lanes(device, lanes, memoryBudget, jobs, count, results);
+        for (uint32_t i = 0; i < count; ++i)
+            if (results[i].status != 0) throw oc::Error("some builds of the batch failed (see their results)");
     });
 }
 
@@ -1096,7 +1120,7 @@ int ocpi_batch_build_wave(int device, uint32_t waveSize, uint64_t memoryBudget, 
         OcpiBatchTuning t = oc::default_tuning();
         if (waveSize) t.waveSize = waveSize;
         else if (count) t = oc::autotune(device, memoryBudget, jobs, count, 0, nullptr);
-        oc::run_batch_waves(device, t, memoryBudget, jobs, count, results, nullptr);
+        oc::run_batch_tuned(device, t, memoryBudget, jobs, count, results, nullptr);
         for (uint32_t i = 0; i < count; ++i)
             if (results[i].status != 0) throw oc::Error("some builds of the batch failed (see their results)");
     });
@@ -1116,7 +1140,7 @@ int ocpi_batch_build_tuned(int device, uint64_t memoryBudget, OcpiBatchTuning* t
         if (!jobs || !results || !tuning) throw oc::Error("null argument");
         oc::validate_tuning(*tuning);
         int issue = -1;
-        oc::run_batch_waves(device, *tuning, memoryBudget, jobs, count, results, &issue);
+        oc::run_batch_tuned(device, *tuning, memoryBudget, jobs, count, results, &issue);
         tuning->lastIssue = issue == 1 ? 1u : 0u;
         for (uint32_t i = 0; i < count; ++i)
             if (results[i].status != 0) throw oc::Error("some builds of the batch failed (see their results)");

@@ -141,6 +141,7 @@ void Wave::issue() {
             st.n_plans = (uint32_t)refs.size() - st.first_plan;
             st.n_nodes = (uint32_t)n;
             st.balance = sum ? (uint32_t)std::min<uint64_t>(64, (mx * sms_ + sum - 1) / sum) : 1u;
+            st.node_blocks = node_blocks_for(mx);
             off += step_table_bytes(st.n_plans, n);
         }
         // every step's tables in one staged block and one copy
@@ -227,7 +228,9 @@ void Wave::issue_steps(const std::vector<Step>& steps, const std::vector<std::pa
             }
             if (!st.n_nodes) continue;
             check_cuda(cudaMemsetAsync(work_.p, 0, 4, stream_), "memset");
-            launch_subsample_wave(st.args, st.wn, sms_, st.balance, stream_, caps_);
+            ClusterCaps caps = caps_;
+            caps.node_blocks = st.node_blocks;
+            launch_subsample_wave(st.args, st.wn, sms_, st.balance, stream_, caps);
         }
     };
     if (graphs_) {

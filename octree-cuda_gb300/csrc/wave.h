@@ -79,6 +79,7 @@ private:
         size_t table_off = 0;      // byte offset of the step's tables in table_
         uint32_t n_nodes = 0;
         uint32_t balance = 1;
+        uint32_t node_blocks = 16;   // cluster limit from the step's largest node
         uint32_t first_plan = 0;   // the step's (slot, level) entries: refs_[first_plan, first_plan + n_plans)
         uint32_t n_plans = 0;
         SubLevelArgs args{};       // mode, record type and grid of the wave's builds

@@ -90,7 +90,7 @@ class OcpiBatchTuning(ctypes.Structure):
     _fields_ = [
         ("waveSize", ctypes.c_uint32), ("clusterCap", ctypes.c_uint32), ("weightedClusterCap", ctypes.c_uint32),
         ("useGraphs", ctypes.c_uint32), ("trialMs", ctypes.c_double), ("trials", ctypes.c_uint32),
-        ("lastIssue", ctypes.c_uint32),
+        ("lastIssue", ctypes.c_uint32), ("lanes", ctypes.c_uint32),
     ]
 
     def as_dict(self):

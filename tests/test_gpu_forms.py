@@ -81,17 +81,17 @@ def test_wave_batch_equals_builds_alone():
         check_same(w, r, *b)
 
 
-@pytest.mark.parametrize("graphs", [1, 0])
-def test_tuned_waves_equal_builds_alone(graphs):
+@pytest.mark.parametrize("graphs,lanes", [(1, 0), (0, 0), (0, 3)])
+def test_tuned_waves_equal_builds_alone(graphs, lanes):
     """An explicit tuning: waves of 6, cluster caps 2/8, each wave's
-    subsampling captured into one CUDA graph (or launched directly); the
-    last wave ran the way it was asked to, and every result equals its build
-    alone."""
+    subsampling captured into one CUDA graph (or launched directly), or the
+    lane executor with 3 lanes; the last wave ran the way it was asked to, and
+    every result equals its build alone."""
     cases = mixed_cases(13)
     want = [alone(c, g, m) for c, g, m in cases]
     bufs = [buffers(w) for w in want]
     jobs = [job_for(c, g, m, *b, device_bbox=(i % 5 == 0)) for i, ((c, g, m), b) in enumerate(zip(cases, bufs))]
-    tuning = octree_api.OcpiBatchTuning(waveSize=6, clusterCap=2, weightedClusterCap=8, useGraphs=graphs)
+    tuning = octree_api.OcpiBatchTuning(waveSize=6, clusterCap=2, weightedClusterCap=8, useGraphs=graphs, lanes=lanes)
     results = octree_api.batch_build_tuned(jobs, tuning)
     assert tuning.lastIssue == graphs
     for w, r, b in zip(want, results, bufs):
@@ -111,10 +111,11 @@ def test_autotune_chooses_and_caches(tmp_path):
     t = octree_api.batch_autotune(jobs, sample_jobs=10, cache_path=str(cache))
     assert t.trials >= 5 and t.trialMs > 0
     assert 1 <= t.waveSize <= 10 and t.clusterCap in (2, 4, 8) and t.weightedClusterCap in (8, 16)
+    assert t.lanes in (0, 4)
     again = octree_api.batch_autotune(jobs, sample_jobs=10, cache_path=str(cache))
     assert again.as_dict() == t.as_dict()
     line = cache.read_text().split()
-    assert int(line[1]) == t.waveSize and int(line[4]) == t.useGraphs
+    assert int(line[1]) == t.waveSize and int(line[4]) == t.useGraphs and int(line[7]) == t.lanes
     results = octree_api.batch_build_wave(jobs, wave_size=0)
     for w, r, b in zip(want, results, bufs):
         check_same(w, r, *b)

@@ -101,6 +101,9 @@ def test_server_and_batch_argument_errors_without_gpu():
     tuning.clusterCap, tuning.weightedClusterCap = 4, 32
     assert L.ocpi_batch_build_tuned(0, 1 << 30, ctypes.byref(tuning), jobs, 1, res) == -1
     assert b"weightedClusterCap" in L.ocpi_last_error()
+    tuning.lanes = 65
+    assert L.ocpi_batch_build_tuned(0, 1 << 30, ctypes.byref(tuning), jobs, 1, res) == -1
+    assert b"lanes" in L.ocpi_last_error()
     t = ctypes.c_uint64()
     assert L.ocpi_server_submit(None, ctypes.byref(octree_api.OcpiJob()), ctypes.byref(t)) == -1
     assert L.ocpi_server_wait(None, 1, None) == -1
@@ -116,7 +119,8 @@ def test_job_structs_match_the_header(tmp_path):
     if not cc:
         pytest.skip("no C compiler")
     fields = {"OcpiJob": [f for f, _ in octree_api.OcpiJob._fields_],
-              "OcpiJobResult": [f for f, _ in octree_api.OcpiJobResult._fields_]}
+              "OcpiJobResult": [f for f, _ in octree_api.OcpiJobResult._fields_],
+              "OcpiBatchTuning": [f for f, _ in octree_api.OcpiBatchTuning._fields_]}
     src = ['#include <stdio.h>', '#include <stddef.h>', '#include "octreeApi.h"', 'int main(void) {']
     for st, fs in fields.items():
         src.append('printf("%%zu\\n", sizeof(%s));' % st)
@@ -128,7 +132,7 @@ def test_job_structs_match_the_header(tmp_path):
     subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(c), "-o", str(exe)], check=True)
     got = [int(x) for x in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
     want = []
-    for st in (octree_api.OcpiJob, octree_api.OcpiJobResult):
+    for st in (octree_api.OcpiJob, octree_api.OcpiJobResult, octree_api.OcpiBatchTuning):
         want.append(ctypes.sizeof(st))
         want += [getattr(st, f).offset for f, _ in st._fields_]
     assert got == want
