@@ -412,7 +412,7 @@ def run_batched(args):
         # the autotuner's trials run on a sample of this batch, outside the
         # timed region
         t0 = time.perf_counter()
-        tuning = octree_api.batch_autotune(jobs, memory_budget=args.budget_gb << 30, sample_jobs=48)
+        tuning = octree_api.batch_autotune(jobs, memory_budget=args.budget_gb << 30)
         tune_s = time.perf_counter() - t0
 
     def batch_pass():

@@ -252,7 +252,9 @@ typedef struct OcpiBatchTuning {
 } OcpiBatchTuning;
 
 /* Measures the batched form on an evenly spaced sample of the jobs (at most
- * sampleJobs of them, 0: 48; their output arrays are written): subsampling
+ * sampleJobs of them, 0: 256, so that a batch of up to 256 jobs is measured
+ * whole: a sample's memory envelope can hide the admission churn of the full
+ * batch; their output arrays are written): subsampling
  * waves over a sweep of wave sizes, cluster caps and graph capture, and the
  * lane executor with 4 lanes; returns the fastest in `tuning`.  The choice is kept for the rest of the process per
  * device and batch signature (job count, mean size, share of float64 clouds,

@@ -987,7 +987,7 @@ OcpiBatchTuning autotune(int device, uint64_t budget, const OcpiJob* jobs, uint3
             return best;
         }
     }
-    const uint32_t m = std::min<uint32_t>(count, sample_jobs ? sample_jobs : 48);
+    const uint32_t m = std::min<uint32_t>(count, sample_jobs ? sample_jobs : 256);
     std::vector<OcpiJob> sample(m);
     for (uint32_t k = 0; k < m; ++k) sample[k] = jobs[(uint64_t)k * count / m];
     std::vector<OcpiJobResult> res(m);
