@@ -338,6 +338,7 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a0, W
     __shared__ uint32_t s_bricks, s_overflow;
     __shared__ uint32_t s_run_total, s_run_off;   // weighted: this block's run of cells in the CSR scan
     __shared__ uint32_t s_skip_node;               // wave: the node's build overflowed a buffer
+    __shared__ uint32_t s_emit_next;               // emit: the next run of 32 cells a warp takes
     const uint32_t csize = kCluster ? cg::this_cluster().num_blocks() : 1u;
     const uint32_t crank = kCluster ? cg::this_cluster().block_rank() : 0u;
     const uint32_t tid0 = crank * blockDim.x + threadIdx.x;   // this thread's index within the node's workers
@@ -381,6 +382,7 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a0, W
     constexpr bool averaged = intra || inter;
 
     uint32_t* p_skip_node = owner(&s_skip_node);
+    uint32_t* p_emit_next = owner(&s_emit_next);
     for (;;) {
         if (crank == 0 && threadIdx.x == 0) {
             const uint32_t k = atomicAdd(a0.work_counter, 1u);
@@ -595,6 +597,7 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a0, W
             }
         }
         const uint32_t cells = ns0->cells;
+        if (crank == 0 && threadIdx.x == 0) s_emit_next = 0;
         for (uint32_t r = tid0; r < cells; r += tstride) {
             a.acc_best[off + r] = ~0ull;
             if (averaged && !weighted) a.acc_intra[off + r] = 0;
@@ -713,9 +716,15 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a0, W
             sync_all();
         }
 
-        // ---- emit one record per occupied cell (thread per cell, rank order;
-        // each warp writes 32 consecutive records with coalesced stores)
-        for (uint32_t r0 = tid0 & ~31u; r0 < cells; r0 += tstride) {
+        // ---- emit one record per occupied cell (thread per cell; each warp
+        // takes the next run of 32 consecutive cells until none is left, so
+        // that warps with light cells take more runs, and writes their
+        // records with coalesced stores)
+        for (;;) {
+            uint32_t r0 = 0;
+            if ((threadIdx.x & 31) == 0) r0 = atomicAdd(p_emit_next, 32u);
+            r0 = __shfl_sync(0xffffffffu, r0, 0);
+            if (r0 >= cells) break;
             const uint32_t r = r0 + (threadIdx.x & 31);
             uint32_t nw[5] = {0, 0, 0, 0, 0};
             if (r < cells) {
