@@ -401,20 +401,6 @@ struct __align__(2) Record18 {   // OutputBuffer, types.cuh:18-24 (packed, 18 by
     uint16_t h[9];
 };
 
-__device__ __forceinline__ void store_record(uint8_t* base, uint64_t pos, int32_t x, int32_t y, int32_t z, uint16_t r,
-                                             uint16_t g, uint16_t b) {
-    uint16_t* p = reinterpret_cast<uint16_t*>(base + pos * 18);
-    p[0] = (uint16_t)x;
-    p[1] = (uint16_t)((uint32_t)x >> 16);
-    p[2] = (uint16_t)y;
-    p[3] = (uint16_t)((uint32_t)y >> 16);
-    p[4] = (uint16_t)z;
-    p[5] = (uint16_t)((uint32_t)z >> 16);
-    p[6] = r;
-    p[7] = g;
-    p[8] = b;
-}
-
 // Record loads.  A 15- or 27-byte record starts at any byte; it is read as
 // the 8-byte-aligned words that cover it (3 words for 15 bytes, 5 for 27) and
 // realigned with funnel shifts.  Memory (global or shared) must be readable up
@@ -626,6 +612,21 @@ __device__ __forceinline__ void store_run(uint8_t* dst, uint32_t r0, uint32_t le
         *reinterpret_cast<uint16_t*>(dst - h + bytes - 2) = *reinterpret_cast<const uint16_t*>(stage + bytes - 2);
     for (uint32_t w = (h >> 1) + lane; w < (bytes >> 2); w += 32) gw[w] = sw[w];
     __syncwarp();
+}
+
+// Stores one 18-byte record n = {x, y, z, r | g << 16, b} at slot pos of a
+// 4-byte aligned record array with five stores: four aligned words and one
+// 2-byte store, at the record's end (even slot) or start (odd slot).  The
+// same instructions run for either parity.
+__device__ __forceinline__ void store_record_words(uint8_t* base, uint64_t pos, const uint32_t (&n)[5]) {
+    uint8_t* p = base + pos * 18;
+    const bool odd = (pos & 1) != 0;
+    *reinterpret_cast<uint16_t*>(p + (odd ? 0 : 16)) = (uint16_t)(odd ? n[0] : n[4]);
+    uint32_t* q = reinterpret_cast<uint32_t*>(p + (odd ? 2 : 0));
+    q[0] = odd ? __funnelshift_r(n[0], n[1], 16) : n[0];
+    q[1] = odd ? __funnelshift_r(n[1], n[2], 16) : n[1];
+    q[2] = odd ? __funnelshift_r(n[2], n[3], 16) : n[2];
+    q[3] = odd ? __funnelshift_r(n[3], n[4], 16) : n[3];
 }
 
 #endif   // __CUDACC__

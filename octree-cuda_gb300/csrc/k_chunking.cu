@@ -41,8 +41,8 @@ __device__ __forceinline__ void set_error(uint32_t* err, uint32_t bit) {
 // counting: 1024-record tiles, 512 threads
 constexpr uint32_t kCountTile = 1024;
 constexpr uint32_t kCountThreads = 512;
-// distribution: 896-record tiles, 448 threads and a record staging area per
-// warp (three blocks fit one SM with float64 records)
+// distribution: 896-record tiles, 448 threads (three blocks fit one SM's
+// registers)
 constexpr uint32_t kDistTile = 896;
 constexpr uint32_t kDistThreads = 448;
 
@@ -51,20 +51,18 @@ __host__ __device__ inline uint32_t align_up(uint32_t x, uint32_t a) {
 }
 
 // Shared-memory layout: [0, 16) two mbarriers, [16, 20) abort flag, then the
-// boundary keys of the three axes, the Morton spread table, the per-warp
-// staging areas and two tile buffers.  A buffer holds a tile's byte span
-// rounded out to 16 bytes plus read slack.
+// boundary keys of the three axes, the Morton spread table and two tile
+// buffers.  A buffer holds a tile's byte span rounded out to 16 bytes plus
+// read slack.
 struct ChunkSmem {
-    uint32_t keys_off, spread_off, stage_off, buf_off, buf_bytes, total;
+    uint32_t keys_off, spread_off, buf_off, buf_bytes, total;
 };
 
-__host__ __device__ inline ChunkSmem chunk_smem(uint32_t stride, uint32_t grid, bool f32, uint32_t tile,
-                                                uint32_t stage_bytes) {
+__host__ __device__ inline ChunkSmem chunk_smem(uint32_t stride, uint32_t grid, bool f32, uint32_t tile) {
     ChunkSmem m;
     m.keys_off = 128;
     m.spread_off = align_up(m.keys_off + 3 * (grid + 2) * (f32 ? 4u : 8u), 16);
-    m.stage_off = align_up(m.spread_off + grid * 4, 128);
-    m.buf_off = align_up(m.stage_off + stage_bytes, 128);
+    m.buf_off = align_up(m.spread_off + grid * 4, 128);
     m.buf_bytes = align_up(tile * stride + 48, 128);
     m.total = m.buf_off + 2 * m.buf_bytes;
     return m;
@@ -192,7 +190,7 @@ __global__ void __launch_bounds__(kCountThreads) k_count(const uint8_t* __restri
                                                          CloudGrid g, uint32_t* __restrict__ pyr0, uint8_t* occ,
                                                          uint32_t* err) {
     extern __shared__ __align__(128) uint8_t smem[];
-    const ChunkSmem L = chunk_smem(stride, g.grid, kF32, kCountTile, 0);
+    const ChunkSmem L = chunk_smem(stride, g.grid, kF32, kCountTile);
     load_tables<kF32>(g, smem, L);
     const uint32_t lane = threadIdx.x & 31;
     tile_loop<kCountTile>(cloud, n, stride, smem, L, err, [&](const uint8_t* recs, uint64_t p0, uint32_t cnt) {
@@ -517,10 +515,9 @@ __global__ void __launch_bounds__(kDistThreads) k_distribute(const uint8_t* __re
                                                               uint32_t* __restrict__ lut, uint8_t* __restrict__ rec,
                                                               uint32_t* __restrict__ frac, uint32_t* err) {
     extern __shared__ __align__(128) uint8_t smem[];
-    const ChunkSmem L = chunk_smem(stride, g.grid, kF32, kDistTile, (kDistThreads / 32) * kStageBytes);
+    const ChunkSmem L = chunk_smem(stride, g.grid, kF32, kDistTile);
     load_tables<kF32>(g, smem, L);
     const uint32_t lane = threadIdx.x & 31;
-    uint8_t* stage = smem + L.stage_off + (threadIdx.x >> 5) * kStageBytes;
     tile_loop<kDistTile>(cloud, n, stride, smem, L, err, [&](const uint8_t* recs, uint64_t p0, uint32_t cnt) {
 #pragma unroll 1
         for (uint32_t base = 0; base < kDistTile; base += kDistThreads) {
@@ -581,26 +578,11 @@ __global__ void __launch_bounds__(kDistThreads) k_distribute(const uint8_t* __re
                     nw[4] = (col >> 16) & 0xFFu;
                 }
             }
-            // records: each run of lanes bound for one leaf fills a contiguous
-            // range; warps with many runs store per lane
-            const uint32_t okmask = __ballot_sync(0xffffffffu, ok);
-            uint32_t runs = starts & okmask;
-            if (__popc(runs) <= 4) {
-                while (runs) {
-                    const uint32_t r0 = __ffs(runs) - 1;
-                    runs &= runs - 1;
-                    const uint32_t above = starts & ~(0xffffffffu >> (31 - r0));
-                    const uint32_t len = (above ? (uint32_t)__ffs(above) - 1 : 32u) - r0;
-                    const uint64_t f = ((uint64_t)__shfl_sync(0xffffffffu, (uint32_t)(first >> 32), r0) << 32) |
-                                       __shfl_sync(0xffffffffu, (uint32_t)first, r0);
-                    if (f + len <= n && ((okmask >> r0) & ((len == 32) ? 0xffffffffu : ((1u << len) - 1))) ==
-                                            ((len == 32) ? 0xffffffffu : ((1u << len) - 1)))
-                        store_run(rec + f * 18, r0, len, nw, stage);
-                }
-            } else if (ok) {
-                store_record(rec, first + (lane - leader), (int32_t)nw[0], (int32_t)nw[1], (int32_t)nw[2],
-                             (uint16_t)(nw[3] & 0xFFFFu), (uint16_t)(nw[3] >> 16), (uint16_t)nw[4]);
-            }
+            // each lane stores its own record with five stores (staging the
+            // runs of a leaf through shared memory for coalesced stores was
+            // slower: 119.7M-point build 3.00 -> 2.73 ms, 25.8M-point random
+            // planes 2.25 -> 1.32 ms)
+            if (ok) store_record_words(rec, first + (lane - leader), nw);
         }
     });
 }
@@ -724,7 +706,7 @@ static int chunk_grid_size(Kernel kernel, uint32_t threads, uint32_t tile, size_
 int launch_count(const uint8_t* cloud, uint64_t n, uint32_t stride, bool float_input, const CloudGrid& g,
                   uint32_t* pyr0, uint8_t* occ, uint32_t* err, int num_sms, cudaStream_t stream) {
     if (n == 0) return 0;
-    const size_t smem = chunk_smem(stride, g.grid, float_input, kCountTile, 0).total;
+    const size_t smem = chunk_smem(stride, g.grid, float_input, kCountTile).total;
     if (float_input) {
         const int grid = chunk_grid_size(k_count<true>, kCountThreads, kCountTile, smem, n, num_sms);
         k_count<true><<<grid, kCountThreads, smem, stream>>>(cloud, n, stride, g, pyr0, occ, err);
@@ -819,7 +801,7 @@ int launch_distribute(const uint8_t* cloud, uint64_t n, uint32_t stride, bool fl
                       uint32_t* lut, uint8_t* rec, uint32_t* frac, uint32_t* err, int num_sms,
                       cudaStream_t stream) {
     if (n == 0) return 0;
-    const size_t smem = chunk_smem(stride, g.grid, float_input, kDistTile, (kDistThreads / 32) * kStageBytes).total;
+    const size_t smem = chunk_smem(stride, g.grid, float_input, kDistTile).total;
     if (float_input) {
         const int grid = chunk_grid_size(k_distribute<true>, kDistThreads, kDistTile, smem, n, num_sms);
         k_distribute<true><<<grid, kDistThreads, smem, stream>>>(cloud, n, stride, g, out, pyr0, data_idx, fill, lut,

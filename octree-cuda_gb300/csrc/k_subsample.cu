@@ -26,8 +26,10 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <map>
 #include <mutex>
 #include <set>
+#include <tuple>
 #include <utility>
 
 #include "device_common.cuh"
@@ -449,19 +451,28 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a0, W
                 const uint32_t* src_lut = ((ns.kind >> c) & 1u) ? a.stage_lut : a.leaf_lut;
                 const uint16_t* src_rec = reinterpret_cast<const uint16_t*>(((ns.kind >> c) & 1u) ? a.stage_rec : a.leaf_rec);
                 const uint32_t* src_frac = ((ns.kind >> c) & 1u) ? a.stage_frac : a.leaf_frac;
-                for (uint32_t k = tid0; k < cnt; k += tstride) {
-                    if (*(volatile uint32_t*)p_overflow) break;
+                // x, y, z of the 18-byte record (2-byte aligned) as four aligned
+                // words, and the candidate's sub-step word
+                auto words = [&](uint32_t k, uint32_t (&w)[5]) {
+                    const uint32_t* rw = reinterpret_cast<const uint32_t*>(
+                        reinterpret_cast<uintptr_t>(src_rec + (start + k) * 9) & ~(uintptr_t)3);
+                    w[0] = rw[0];
+                    w[1] = rw[1];
+                    w[2] = rw[2];
+                    w[3] = rw[3];
+                    w[4] = src_frac ? src_frac[start + k] : 0u;
+                };
+                // Cell and occupancy of candidate k; false when the node
+                // overflows the table.  The cell comes from the record's
+                // quantised coordinates; the cloud point is read only when a
+                // quantisation step straddles a cell boundary.
+                auto place = [&](uint32_t k, const uint32_t (&w)[5]) -> bool {
                     const uint32_t j = jbase + k;
-                    // cell from the record's quantised coordinates; the cloud point
-                    // is read only when a quantisation step straddles a boundary
-                    // x, y, z of the 18-byte record (2-byte aligned) from four aligned words
-                    const uintptr_t ra = reinterpret_cast<uintptr_t>(src_rec + (start + k) * 9);
-                    const uint32_t* rw = reinterpret_cast<const uint32_t*>(ra & ~(uintptr_t)3);
-                    const uint32_t rs = (uint32_t)(ra & 2) * 8;
-                    const uint32_t w0 = rw[0], w1 = rw[1], w2 = rw[2], w3 = rw[3];
-                    const int32_t q0 = (int32_t)__funnelshift_r(w0, w1, rs), q1 = (int32_t)__funnelshift_r(w1, w2, rs),
-                                  q2 = (int32_t)__funnelshift_r(w2, w3, rs);
-                    const uint32_t fw = src_frac ? src_frac[start + k] : 0u;
+                    const uint32_t rs = (uint32_t)(reinterpret_cast<uintptr_t>(src_rec + (start + k) * 9) & 2) * 8;
+                    const int32_t q0 = (int32_t)__funnelshift_r(w[0], w[1], rs),
+                                  q1 = (int32_t)__funnelshift_r(w[1], w[2], rs),
+                                  q2 = (int32_t)__funnelshift_r(w[2], w[3], rs);
+                    const uint32_t fw = w[4];
                     int ix, iy, iz;
                     if (fw >> 31) {
                         ix = quant_cell_fine(q0, fw & 1023u, qa0, a.grid);
@@ -495,7 +506,7 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a0, W
                     if (fresh && atomicAdd(p_bricks, 1u) + 1 >= limit) *(volatile uint32_t*)p_overflow = 1;
                     if (slot >= bm.cap) {
                         *(volatile uint32_t*)p_overflow = 1;
-                        break;
+                        return false;
                     }
                     // 32-bit atomic on the half of the mask that holds the bit
                     atomicOr(reinterpret_cast<uint32_t*>(&bm.mask[slot]) + (bit >> 5), 1u << (bit & 31));
@@ -511,6 +522,19 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a0, W
                         a.unit_cache[(off + j) * 3 + 1] = point_units<kF32>(co[1], ax1);
                         a.unit_cache[(off + j) * 3 + 2] = point_units<kF32>(co[2], ax2);
                     }
+                    return true;
+                };
+                // two candidates per thread per iteration, both records loaded
+                // before either is placed (119.7M-point build: subsampling
+                // 13.6 -> 13.1 ms)
+                for (uint32_t k = tid0; k < cnt; k += 2 * tstride) {
+                    if (*(volatile uint32_t*)p_overflow) break;
+                    const uint32_t k2 = k + tstride;
+                    uint32_t w[5], v[5] = {0, 0, 0, 0, 0};
+                    words(k, w);
+                    if (k2 < cnt) words(k2, v);
+                    if (!place(k, w)) break;
+                    if (k2 < cnt && !place(k2, v)) break;
                 }
             }
             sync_all();
@@ -613,11 +637,22 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a0, W
             const bool staged = (ns.kind >> c) & 1u;
             const uint32_t* src_lut = staged ? a.stage_lut : a.leaf_lut;
             const uint8_t* src_rec = staged ? a.stage_rec : a.leaf_rec;
-            for (uint32_t k = tid0; k < cnt; k += tstride) {
-                const uint32_t kc = a.key_cache[off + jbase + k];
-                const uint32_t slot = kc >> 6, bit = kc & 63;
+            // candidate k's cell word, cloud index and (averaged modes) the two
+            // aligned words holding r, g, b (bytes 12..17 of the record)
+            auto loads = [&](uint32_t k, uint32_t (&w)[4]) {
+                w[0] = a.key_cache[off + jbase + k];
+                w[1] = src_lut[start + k];
+                if (averaged && !weighted) {
+                    const uint32_t* cw = reinterpret_cast<const uint32_t*>(
+                        reinterpret_cast<uintptr_t>(src_rec + (start + k) * 18 + 12) & ~(uintptr_t)3);
+                    w[2] = cw[0];
+                    w[3] = cw[1];
+                }
+            };
+            auto take = [&](uint32_t k, const uint32_t (&w)[4]) {
+                const uint32_t slot = w[0] >> 6, bit = w[0] & 63;
                 const uint32_t rank = bm.base[slot] + (uint32_t)__popcll(bm.mask[slot] & ((1ull << bit) - 1ull));
-                const uint32_t idx = src_lut[start + k];
+                const uint32_t idx = w[1];
                 // first point: (cloud index, candidate) -- the smallest index wins and
                 // carries its candidate position; explicit random: (priority, index)
                 uint64_t key;
@@ -625,17 +660,23 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a0, W
                 else key = ((uint64_t)idx << 32) | (jbase + k);
                 atomicMin(reinterpret_cast<unsigned long long*>(&a.acc_best[off + rank]), (unsigned long long)key);
                 if (averaged && !weighted) {
-                    // r, g, b (bytes 12..17 of the record) from two aligned words
-                    const uintptr_t ca = reinterpret_cast<uintptr_t>(src_rec + (start + k) * 18 + 12);
-                    const uint32_t* cw = reinterpret_cast<const uint32_t*>(ca & ~(uintptr_t)3);
-                    const uint32_t cs = (uint32_t)(ca & 2) * 8;
-                    const uint32_t c0 = cw[0], c1 = cw[1];
-                    const uint32_t rg = __funnelshift_r(c0, c1, cs);
-                    const uint32_t bb = (c1 >> cs) & 0xFFFFu;
+                    const uint32_t cs = (uint32_t)(reinterpret_cast<uintptr_t>(src_rec + (start + k) * 18 + 12) & 2) * 8;
+                    const uint32_t rg = __funnelshift_r(w[2], w[3], cs);
+                    const uint32_t bb = (w[3] >> cs) & 0xFFFFu;
                     const uint64_t enc = encode_colors(rg & 0xFFFFu, rg >> 16, bb);
                     atomicAdd(reinterpret_cast<unsigned long long*>(&a.acc_intra[off + rank]), (unsigned long long)enc);
                 }
                 if (weighted) atomicAdd(&a.csr_count[off + rank], 1u);
+            };
+            // two candidates per thread per iteration, loads first (119.7M-point
+            // build: subsampling 13.6 -> 12.8 ms, 12.4 ms with pass A's pairs)
+            for (uint32_t k = tid0; k < cnt; k += 2 * tstride) {
+                const uint32_t k2 = k + tstride;
+                uint32_t w[4] = {0, 0, 0, 0}, v[4] = {0, 0, 0, 0};
+                loads(k, w);
+                if (k2 < cnt) loads(k2, v);
+                take(k, w);
+                if (k2 < cnt) take(k2, v);
             }
         }
         sync_all();
@@ -738,8 +779,11 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a0, W
                 const uint32_t jsel = random ? a.acc_sel[off + r] : (uint32_t)best;
                 // the winner's record holds its output coordinates (same cloud
                 // minimum and scale at every level) and, unaveraged, its colour
+                // the child holding candidate jsel: a count of comparisons, the
+                // same instructions on every lane
                 uint32_t csel = 0;
-                while (csel + 1 < ns.nchild && ns.prefix[csel + 1] <= jsel) ++csel;
+#pragma unroll
+                for (uint32_t c = 1; c < 8; ++c) csel += (c < ns.nchild && ns.prefix[c] <= jsel) ? 1u : 0u;
                 const uint64_t spos = ns.start[csel] + (jsel - ns.prefix[csel]);
                 const uintptr_t sa =
                     reinterpret_cast<uintptr_t>((((ns.kind >> csel) & 1u) ? a.stage_rec : a.leaf_rec) + spos * 18);
@@ -875,13 +919,84 @@ uint32_t cluster_size(uint32_t n_nodes, int num_sms, uint32_t cap) {
     return c;
 }
 
+// Clusters of c blocks of `kernel` that the device holds at once (0: none
+// fits).  A cluster must fit in one GPC, so the count follows how the chip's
+// SMs are grouped and differs between GPUs of one model (clusters of 16 are
+// the sensitive size).  Queried once per device, kernel and size.
+int cluster_slots(const void* kernel, size_t smem, uint32_t c) {
+    static std::mutex mu;
+    static std::map<std::tuple<int, const void*, uint32_t>, int> known;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const auto key = std::make_tuple(dev, kernel, c);
+    {
+        std::lock_guard<std::mutex> g(mu);
+        auto it = known.find(key);
+        if (it != known.end()) return it->second;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = c;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(c);
+    cfg.blockDim = dim3(kSubThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int m = 0;
+    if (cudaOccupancyMaxActiveClusters(&m, kernel, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        m = 0;
+    }
+    std::lock_guard<std::mutex> g(mu);
+    known[key] = m;
+    return m;
+}
+
+// Cluster size for a distance-weighted level: the c (1 to cap) with the
+// smallest estimated level time
+//     max(1 / resident blocks(c), r / c) * g(c)
+// where resident blocks(c) = min(n_nodes, slots(c)) * c, r = the largest
+// node's share of the level's candidates (balance / num_sms) and g(c) the
+// per-block cost of cluster-wide work, fitted to measured levels: one-node
+// and 8-node levels of the 25.8M-point weighted build ran 1.29x and 1.74x
+// (root) and 1.62x and 2.15x (8 nodes) longer per block at clusters of 8 and
+// 16 than at 4, about c^0.4.  On a GPU that holds 9 clusters of 16 this
+// gives the largest node at least its share of the blocks, the rule used
+// before; on one that holds fewer, many-node levels take smaller clusters.
+uint32_t weighted_cluster_size(const void* cluster_kernel, size_t smem, uint32_t n_nodes, int num_sms,
+                               uint32_t balance, uint32_t cap) {
+    static const double g[5] = {1.0, 1.32, 1.74, 2.30, 3.03};
+    const double r = (double)balance / (double)std::max(num_sms, 1);
+    uint32_t best = 1;
+    double best_t = std::max(1.0 / (double)std::min<uint32_t>(n_nodes, (uint32_t)num_sms), r);
+    int i = 1;
+    for (uint32_t c = 2; c <= cap && i < 5; c <<= 1, ++i) {
+        const int s = cluster_slots(cluster_kernel, smem, c);
+        if (s <= 0) break;
+        const double blocks = (double)std::min<uint32_t>(n_nodes, (uint32_t)s) * c;
+        const double t = std::max(1.0 / blocks, r / c) * g[i];
+        if (t < best_t) {
+            best_t = t;
+            best = c;
+        }
+    }
+    return best;
+}
+
 template <bool kF32, int kColor, bool kRandom, bool kWave>
 void launch_one(const SubLevelArgs& a, const WaveNodes& wn, int num_sms, uint32_t balance, size_t smem,
                 cudaStream_t stream, const ClusterCaps& caps) {
     const uint32_t cap = std::min(kColor == 3 ? caps.weighted : caps.plain, std::max(caps.node_blocks, 1u));
     uint32_t cs = cluster_size(a.n_nodes, num_sms, cap);
-    if (kColor == 3)
-        while (cs < cap && cs < balance) cs <<= 1;
+    if (kColor == 3 && cap > 1) {
+        auto kern = k_subsample<kF32, kColor, kRandom, true, kWave>;
+        allow_dynamic_smem(reinterpret_cast<const void*>(kern), smem);
+        if (cap > 8) allow_wide_clusters(reinterpret_cast<const void*>(kern));
+        cs = weighted_cluster_size(reinterpret_cast<const void*>(kern), smem, a.n_nodes, num_sms, balance, cap);
+    }
     if (cs > 1) {
         auto kern = k_subsample<kF32, kColor, kRandom, true, kWave>;
         allow_dynamic_smem(reinterpret_cast<const void*>(kern), smem);
@@ -899,9 +1014,8 @@ void launch_one(const SubLevelArgs& a, const WaveNodes& wn, int num_sms, uint32_
         // the largest cluster size up to cs of which one cluster fits
         for (uint32_t c = cs; c > 1; c >>= 1) {
             attr[0].val.clusterDim.x = c;
-            cfg.gridDim = dim3(c);
-            int max_clusters = 0;
-            if (cudaOccupancyMaxActiveClusters(&max_clusters, kern, &cfg) == cudaSuccess && max_clusters > 0) {
+            const int max_clusters = cluster_slots(reinterpret_cast<const void*>(kern), smem, c);
+            if (max_clusters > 0) {
                 const uint32_t clusters = std::min<uint32_t>(a.n_nodes, (uint32_t)max_clusters);
                 cfg.gridDim = dim3(clusters * c);
                 if (cudaLaunchKernelEx(&cfg, kern, a, wn) == cudaSuccess) return;
