@@ -526,15 +526,17 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a0, W
                 };
                 // two candidates per thread per iteration, both records loaded
                 // before either is placed (119.7M-point build: subsampling
-                // 13.6 -> 13.1 ms)
-                for (uint32_t k = tid0; k < cnt; k += 2 * tstride) {
+                // 13.6 -> 13.1 ms); one for distance weighting, whose pass also
+                // reads the cloud point (pairs: 25.8M-point build 21.8 -> 22.3 ms)
+                for (uint32_t k = tid0; k < cnt; k += (weighted ? 1u : 2u) * tstride) {
                     if (*(volatile uint32_t*)p_overflow) break;
                     const uint32_t k2 = k + tstride;
+                    const bool two = !weighted && k2 < cnt;
                     uint32_t w[5], v[5] = {0, 0, 0, 0, 0};
                     words(k, w);
-                    if (k2 < cnt) words(k2, v);
+                    if (two) words(k2, v);
                     if (!place(k, w)) break;
-                    if (k2 < cnt && !place(k2, v)) break;
+                    if (two && !place(k2, v)) break;
                 }
             }
             sync_all();
@@ -669,14 +671,16 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a0, W
                 if (weighted) atomicAdd(&a.csr_count[off + rank], 1u);
             };
             // two candidates per thread per iteration, loads first (119.7M-point
-            // build: subsampling 13.6 -> 12.8 ms, 12.4 ms with pass A's pairs)
-            for (uint32_t k = tid0; k < cnt; k += 2 * tstride) {
+            // build: subsampling 13.6 -> 12.8 ms, 12.3 ms with pass A's pairs);
+            // one for distance weighting
+            for (uint32_t k = tid0; k < cnt; k += (weighted ? 1u : 2u) * tstride) {
                 const uint32_t k2 = k + tstride;
+                const bool two = !weighted && k2 < cnt;
                 uint32_t w[4] = {0, 0, 0, 0}, v[4] = {0, 0, 0, 0};
                 loads(k, w);
-                if (k2 < cnt) loads(k2, v);
+                if (two) loads(k2, v);
                 take(k, w);
-                if (k2 < cnt) take(k2, v);
+                if (two) take(k2, v);
             }
         }
         sync_all();
@@ -777,13 +781,13 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a0, W
                 const uint64_t best = a.acc_best[off + r];
                 const uint32_t idx = random ? (uint32_t)best : (uint32_t)(best >> 32);
                 const uint32_t jsel = random ? a.acc_sel[off + r] : (uint32_t)best;
-                // the winner's record holds its output coordinates (same cloud
-                // minimum and scale at every level) and, unaveraged, its colour
                 // the child holding candidate jsel: a count of comparisons, the
                 // same instructions on every lane
                 uint32_t csel = 0;
 #pragma unroll
                 for (uint32_t c = 1; c < 8; ++c) csel += (c < ns.nchild && ns.prefix[c] <= jsel) ? 1u : 0u;
+                // the winner's record holds its output coordinates (same cloud
+                // minimum and scale at every level) and, unaveraged, its colour
                 const uint64_t spos = ns.start[csel] + (jsel - ns.prefix[csel]);
                 const uintptr_t sa =
                     reinterpret_cast<uintptr_t>((((ns.kind >> csel) & 1u) ? a.stage_rec : a.leaf_rec) + spos * 18);
