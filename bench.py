@@ -803,9 +803,10 @@ def main():
                 "init_ms": [round(x * 1e3, 2) for x in init_times], **link},
         "clocks": clk,
         "reference_cuda": {"available": False,
-                           "reason": "the reference's own CUDA pipeline, compiled unmodified for sm_103a, faulted "
-                                     "(illegal memory access) on every cloud it was given on this GPU; it is not "
-                                     "run again"},
+                           "reason": "the reference's own CUDA pipeline, compiled unmodified for sm_103a, did not "
+                                     "complete on this GPU: its subsampling reads node fields that nothing "
+                                     "initialises and accesses memory outside its buffers on every cloud it was "
+                                     "given; it is not run again"},
     }
     if rank == 0 and not args.no_cpu_baseline:
         # the oracle builds the same whole cloud on the host cores; its result

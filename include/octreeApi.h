@@ -100,6 +100,9 @@ typedef struct OcpiStats {
     float mean_leaf_points;
     float stdev_leaf_points;
     uint32_t kernel_launches; /* kernels launched by the last ocpi_generate_octree */
+    uint32_t subsample_passes; /* subsampling passes of the last build: 1, or more when a level's
+                                  candidates or the final records outgrew their buffers and the
+                                  pass was repeated with larger ones */
 } OcpiStats;
 
 OCPI_EXPORT int ocpi_get_stats(void* session, OcpiStats* out);
@@ -197,6 +200,8 @@ typedef struct OcpiJobResult {
     double totalMs;            /* submission to completion */
     double deviceMs;           /* build stages, CUDA events */
     char error[128];
+    uint32_t subsamplePasses;  /* as OcpiStats.subsample_passes; a build of a subsampling wave that
+                                  outgrew its buffers repeats its pass alone */
 } OcpiJobResult;
 
 OCPI_EXPORT int ocpi_server_create(void** server, int device, uint32_t lanes, uint64_t memoryBudget);

@@ -1254,6 +1254,7 @@ void Builder::subsample() {
             stage_used_ = *back_host_.as<uint64_t>(8);
             sub_err_ = e;
             sub_err_valid_ = true;
+            stats_.subsample_passes = (uint32_t)attempt + 1;
             break;
         }
         if (attempt >= 6 || (e & ~kErrCapacity)) check_device_errors("subsample");

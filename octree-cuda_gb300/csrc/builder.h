@@ -130,6 +130,7 @@ struct Stats {
     uint32_t max_leaf_depth = 0, min_leaf_points = 0, max_leaf_points = 0;
     float mean_leaf_points = 0.f, stdev_leaf_points = 0.f;
     uint32_t kernel_launches = 0;   // kernels launched by the last generate
+    uint32_t subsample_passes = 0;  // 1, or more when the subsampling pass was repeated with larger buffers
 };
 
 // Upper bound of the device memory a session allocates for a configuration

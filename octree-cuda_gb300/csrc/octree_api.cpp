@@ -331,6 +331,7 @@ int ocpi_get_stats(void* session, OcpiStats* out) {
         o.mean_leaf_points = S.mean_leaf_points;
         o.stdev_leaf_points = S.stdev_leaf_points;
         o.kernel_launches = S.kernel_launches;
+        o.subsample_passes = S.subsample_passes;
         *out = o;
     });
 }

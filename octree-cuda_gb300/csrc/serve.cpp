@@ -546,6 +546,7 @@ private:
                 r.status = 0;
                 r.nodeCount = st.tree_nodes;
                 r.pointsTotal = st.points_total;
+                r.subsamplePasses = st.subsample_passes;
                 for (const auto& t : builder->timings()) r.deviceMs += t.second;
             } catch (const std::exception& e) {
                 r.status = -1;
@@ -696,6 +697,7 @@ OcpiJobResult run_wave_slot(int device, WavePool& pool, Wave& wave, uint32_t q, 
         r.status = 0;
         r.nodeCount = st.tree_nodes;
         r.pointsTotal = st.points_total;
+        r.subsamplePasses = st.subsample_passes;
         for (const auto& t : b->timings()) r.deviceMs += t.second;
     } catch (const std::exception& e) {
         r.status = -1;

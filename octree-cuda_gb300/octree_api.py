@@ -60,6 +60,7 @@ class OcpiStats(ctypes.Structure):
         ("dense_nodes", ctypes.c_uint32), ("max_leaf_depth", ctypes.c_uint32), ("min_leaf_points", ctypes.c_uint32),
         ("max_leaf_points", ctypes.c_uint32), ("mean_leaf_points", ctypes.c_float),
         ("stdev_leaf_points", ctypes.c_float), ("kernel_launches", ctypes.c_uint32),
+        ("subsample_passes", ctypes.c_uint32),
     ]
 
     def as_dict(self):
@@ -83,6 +84,7 @@ class OcpiJobResult(ctypes.Structure):
         ("status", ctypes.c_int32), ("lane", ctypes.c_uint32), ("nodeCount", ctypes.c_uint32),
         ("reused", ctypes.c_uint32), ("pointsTotal", ctypes.c_uint64), ("queuedMs", ctypes.c_double), ("runMs", ctypes.c_double),
         ("totalMs", ctypes.c_double), ("deviceMs", ctypes.c_double), ("error", ctypes.c_char * 128),
+        ("subsamplePasses", ctypes.c_uint32),
     ]
 
 

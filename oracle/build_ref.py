@@ -15,9 +15,9 @@ INFRASTRUCTURE ONLY.
              alias; see that file).  Flags follow the reference's CMake build
              (separable compilation, header-only spdlog) with release
              optimisation.  Compile only: the reference pipeline is not run on a
-             GPU here, because it faulted with an illegal memory access on every
+             GPU here, because it accessed memory outside its buffers on every
              cloud it was given (its subsampling reads node fields that nothing
-             initialises; the design doc records the run and the cause).
+             initialises).
 
     python oracle/build_ref.py            # stage the reader
     python oracle/build_ref.py --compile  # compile the reference library

@@ -81,6 +81,34 @@ def test_wave_batch_equals_builds_alone():
         check_same(w, r, *b)
 
 
+def test_wave_build_that_outgrows_its_buffers_repeats_alone():
+    """A wave build whose records outgrow its buffers leaves the wave's
+    schedule and repeats its subsampling pass alone with larger buffers.
+    Output factor 1.0 sizes the records for N only, and the 1.5M-point cloud
+    is larger than any cloud the wave builders of this process have held, so
+    its first pass overflows.  Every build of the wave equals its build
+    alone, and the large one took a second pass."""
+    cases = [make_case(1, 0, n, seed=3100 + i) for i, n in enumerate((1_500_000, 60_000, 90_000))]
+    grids = (128, 64)
+    want, passes = [], []
+    for c in cases:
+        s = run_gpu(c, dict(chunk_grid=grids[0], sub_grid=grids[1], merge_threshold=2000, seed=99,
+                            output_factor=1.0, **MODES[0]))
+        want.append((s.hierarchy(), s.records(), s.lut()))
+        passes.append(s.stats()["subsample_passes"])
+        s.close()
+    assert passes[0] >= 2, "the session build did not outgrow its buffers"
+    bufs = [buffers(w) for w in want]
+    jobs = [octree_api.make_job(c.cloud, n=c.n, stride=c.stride, cloud_type=c.cloud_type, scale=c.scale,
+                                bb_min=c.bb_min, bb_max=c.bb_max, chunk_grid=grids[0], sub_grid=grids[1],
+                                merge_threshold=2000, output_factor=1.0, flags=FLAGS[0], seed=99,
+                                records=b[0], lut=b[1], hierarchy=b[2]) for c, b in zip(cases, bufs)]
+    results = octree_api.batch_build_wave(jobs, wave_size=3)
+    for w, r, b in zip(want, results, bufs):
+        check_same(w, r, *b)
+    assert results[0].subsamplePasses >= 2
+
+
 @pytest.mark.parametrize("graphs,lanes", [(1, 0), (0, 0), (0, 3)])
 def test_tuned_waves_equal_builds_alone(graphs, lanes):
     """An explicit tuning: waves of 6, cluster caps 2/8, each wave's

@@ -111,7 +111,8 @@ def test_server_and_batch_argument_errors_without_gpu():
 
 
 def test_job_structs_match_the_header(tmp_path):
-    """ctypes layouts of OcpiJob / OcpiJobResult against the C compiler's."""
+    """ctypes layouts of OcpiJob / OcpiJobResult / OcpiBatchTuning / OcpiStats
+    against the C compiler's."""
     import shutil
     import subprocess
 
@@ -120,7 +121,8 @@ def test_job_structs_match_the_header(tmp_path):
         pytest.skip("no C compiler")
     fields = {"OcpiJob": [f for f, _ in octree_api.OcpiJob._fields_],
               "OcpiJobResult": [f for f, _ in octree_api.OcpiJobResult._fields_],
-              "OcpiBatchTuning": [f for f, _ in octree_api.OcpiBatchTuning._fields_]}
+              "OcpiBatchTuning": [f for f, _ in octree_api.OcpiBatchTuning._fields_],
+              "OcpiStats": [f for f, _ in octree_api.OcpiStats._fields_]}
     src = ['#include <stdio.h>', '#include <stddef.h>', '#include "octreeApi.h"', 'int main(void) {']
     for st, fs in fields.items():
         src.append('printf("%%zu\\n", sizeof(%s));' % st)
@@ -132,7 +134,7 @@ def test_job_structs_match_the_header(tmp_path):
     subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(c), "-o", str(exe)], check=True)
     got = [int(x) for x in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
     want = []
-    for st in (octree_api.OcpiJob, octree_api.OcpiJobResult, octree_api.OcpiBatchTuning):
+    for st in (octree_api.OcpiJob, octree_api.OcpiJobResult, octree_api.OcpiBatchTuning, octree_api.OcpiStats):
         want.append(ctypes.sizeof(st))
         want += [getattr(st, f).offset for f, _ in st._fields_]
     assert got == want
