@@ -506,9 +506,11 @@ __global__ void k_push_tags(uint32_t* __restrict__ pyr, const uint64_t* __restri
 // K5 (point_distributing.cuh:30-75): every point goes to its leaf's bucket
 // with its LUT entry and 18-byte output record.  The first lane of each run
 // of equal cells reads the cell's leaf tag; the first lane of each run of
-// equal leaves reserves the run's slots with one atomic.
+// equal leaves reserves the run's slots with one atomic.  At most 40
+// registers, so that three 448-thread blocks share an SM (47 registers leave
+// room for two: 119.7M-point build 2.73 -> 2.56 ms).
 template <bool kF32>
-__global__ void __launch_bounds__(kDistThreads) k_distribute(const uint8_t* __restrict__ cloud, uint64_t n,
+__global__ void __launch_bounds__(kDistThreads, 3) k_distribute(const uint8_t* __restrict__ cloud, uint64_t n,
                                                               uint32_t stride, CloudGrid g, OutParams op,
                                                               const uint32_t* __restrict__ pyr0,
                                                               const uint64_t* __restrict__ data_idx, uint32_t* fill,

@@ -638,6 +638,11 @@ Executor* to_executor(void* p) {
 // a host thread of its own; their subsampling plans meet in the wave, which
 // issues them as one schedule (one launch per level over all of them).
 //
+// Cloud bytes of a job: the order of builds in a batch.
+static uint64_t job_bytes(const OcpiJob& j) {
+    return (uint64_t)j.pointAmount * j.dataStride;
+}
+
 // Two waves are in flight: the pool holds two sets of `slots` builders and
 // two Wave objects, and wave k uses set k mod 2.  While wave k's schedule
 // subsamples, wave k + 1's builds upload, count and distribute; wave k + 2
@@ -751,8 +756,15 @@ void run_batch_waves(int device, const OcpiBatchTuning& tuning, uint64_t budget,
         const bool inter = !c.intra && c.inter;
         groups[std::make_tuple(c.cloud_type, c.intra, inter, inter && c.weighting, c.random)].push_back(i);
     }
-    std::vector<uint32_t> order;   // jobs group by group, in submission order within a group
-    for (auto& kv : groups) order.insert(order.end(), kv.second.begin(), kv.second.end());
+    // jobs group by group, largest cloud first within a group: a wave's
+    // subsampling starts when its last build is ready, so a wave holds builds
+    // of similar size
+    std::vector<uint32_t> order;
+    for (auto& kv : groups) {
+        std::stable_sort(kv.second.begin(), kv.second.end(),
+                         [&](uint32_t a, uint32_t b) { return job_bytes(jobs[a]) > job_bytes(jobs[b]); });
+        order.insert(order.end(), kv.second.begin(), kv.second.end());
+    }
 
     struct Running {
         std::vector<uint32_t> jobs;
@@ -943,7 +955,8 @@ OcpiBatchTuning default_tuning() {
 }   // namespace
 
 // The lane executor on a batch: every job checked before any starts, results
-// in order.
+// in order.  Jobs are submitted largest cloud first, so that the batch does
+// not end on a large build running alone.
 void run_batch_lanes(int device, uint32_t lanes, uint64_t budget, const OcpiJob* jobs, uint32_t count,
                      OcpiJobResult* results) {
     if (lanes < 1 || lanes > 64) throw Error("lanes must be in [1, 64]");
@@ -956,9 +969,12 @@ void run_batch_lanes(int device, uint32_t lanes, uint64_t budget, const OcpiJob*
             throw Error("job " + std::to_string(i) + " of the batch: " + e.what());
         }
     }
+    std::vector<uint32_t> order(count);
+    for (uint32_t i = 0; i < count; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return job_bytes(jobs[a]) > job_bytes(jobs[b]); });
     std::vector<uint64_t> tickets(count);
-    for (uint32_t i = 0; i < count; ++i) tickets[i] = ex.submit(jobs[i]);
-    for (uint32_t i = 0; i < count; ++i) {
+    for (uint32_t i : order) tickets[i] = ex.submit(jobs[i]);
+    for (uint32_t i : order) {
         results[i] = ex.wait(tickets[i]);
         ex.release(tickets[i]);
     }
