@@ -183,6 +183,31 @@ def cpu_oracle_time(cloud, bb, n_sample, threads):
     return cpu_oracle_run(cloud, bb, n_sample, threads)[0]
 
 
+def export_timing(s, points_total):
+    """Wall time of one ocpi_export_potree of the session's build (hierarchy.bin,
+    octree.bin, metadata.json) into a scratch directory, and the bytes it
+    wrote; the files are removed afterwards.  Skipped when the scratch file
+    system lacks twice the room."""
+    import shutil
+    import tempfile
+
+    need = points_total * 18
+    free = shutil.disk_usage(tempfile.gettempdir()).free
+    if free < 2 * need:
+        return {"skipped": "%.1f GB free in %s, %.1f GB to write" % (free / 1e9, tempfile.gettempdir(), need / 1e9)}
+    d = tempfile.mkdtemp(prefix="ocpi_export_")
+    try:
+        t0 = time.perf_counter()
+        s.export_potree(d)
+        dt = time.perf_counter() - t0
+        nbytes = sum(os.path.getsize(os.path.join(d, f)) for f in os.listdir(d))
+        return {"ms": round(dt * 1e3, 1), "bytes": nbytes, "gbs": round(nbytes / dt / 1e9, 2)}
+    except Exception as e:   # a full or read-only scratch disk: reported, not fatal
+        return {"error": str(e)[:200]}
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+
+
 def cpu_oracle_run(cloud, bb, n_sample, threads):
     """Seconds of one oracle build of the first n_sample points, and its result."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -808,6 +833,9 @@ def main():
                                      "initialises and accesses memory outside its buffers on every cloud it was "
                                      "given; it is not run again"},
     }
+    if rank == 0:
+        # Potree export of the last build, outside every timed region
+        line["export"] = export_timing(s, int(st["points_total"]))
     if rank == 0 and not args.no_cpu_baseline:
         # the oracle builds the same whole cloud on the host cores; its result
         # is the check of the GPU build (outside every timed region)
