@@ -965,8 +965,9 @@ namespace {
 // Blocks per node for a level of n_nodes nodes: the smallest power of two up
 // to `cap` whose clusters cover the SMs (levels with at least one node per SM
 // run one block per node).  Measured per level on the 119.7M-point build:
-// clusters of 2 take a 100-node level from 0.54 to 0.34 ms; clusters of 8 are
-// slower than 4 on 10- to 40-node levels, so the cap is 4.  Distance-weighted
+// clusters of 2 take a 100-node level from 0.54 to 0.34 ms; clusters of 8 were
+// slower than 4 on its 10- to 40-node levels, so the cap is 4, and 8 for
+// levels of at most 16 nodes (launch_one).  Distance-weighted
 // levels go up to 16 (a non-portable cluster size), and at least to the
 // level's balance_blocks: the neighbourhood walk per output cell makes a
 // level's largest nodes long.  On the 25.8M-point weighted build a cap of 16
@@ -1061,7 +1062,12 @@ uint32_t weighted_cluster_size(const void* cluster_kernel, size_t smem, uint32_t
 template <bool kF32, int kColor, bool kRandom, bool kWave>
 void launch_one(const SubLevelArgs& a, const WaveNodes& wn, int num_sms, uint32_t balance, size_t smem,
                 cudaStream_t stream, const ClusterCaps& caps) {
-    const uint32_t cap = std::min(kColor == 3 ? caps.weighted : caps.plain, std::max(caps.node_blocks, 1u));
+    // levels of at most 16 nodes (the top of the tree, a few large nodes)
+    // take clusters of up to 8: 25.8M-point random planes 6.70 -> 6.40 ms
+    // (root 0.90 -> 0.68 ms), 5.1M-point heightfield 1.56 -> 1.53 ms; 16
+    // helped the first root further but slowed the other two
+    const uint32_t plain_cap = a.n_nodes <= 16u ? std::max(caps.plain, 8u) : caps.plain;
+    const uint32_t cap = std::min(kColor == 3 ? caps.weighted : plain_cap, std::max(caps.node_blocks, 1u));
     uint32_t cs = cluster_size(a.n_nodes, num_sms, cap);
     if (kColor == 3 && cap > 1) {
         auto kern = k_subsample<kF32, kColor, kRandom, true, kWave>;
