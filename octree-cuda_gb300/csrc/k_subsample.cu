@@ -1046,7 +1046,9 @@ uint32_t weighted_cluster_size(const void* cluster_kernel, size_t smem, uint32_t
     uint32_t best = 1;
     double best_t = std::max(1.0 / (double)std::min<uint32_t>(n_nodes, (uint32_t)num_sms), r);
     int i = 1;
-    for (uint32_t c = 2; c <= cap && i < 5; c <<= 1, ++i) {
+    // never more blocks than the caller's SMs (the allocation-free entry
+    // point subsamples its node in one block)
+    for (uint32_t c = 2; c <= cap && c <= (uint32_t)std::max(num_sms, 1) && i < 5; c <<= 1, ++i) {
         const int s = cluster_slots(cluster_kernel, smem, c);
         if (s <= 0) break;
         const double blocks = (double)std::min<uint32_t>(n_nodes, (uint32_t)s) * c;
