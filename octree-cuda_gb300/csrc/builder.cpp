@@ -505,7 +505,7 @@ std::vector<std::pair<std::string, uint64_t>> Builder::device_allocations() cons
         {"staged LUT", stage_lut_.bytes},
         {"sub-step words", leaf_frac_.bytes + stage_frac_.bytes},
         {"subsampling scratch", key_cache_.bytes + unit_cache_.bytes + acc_best_.bytes + acc_sel_.bytes +
-                                    cell_slot_.bytes + acc_intra_.bytes + acc_w_.bytes + csr_count_.bytes +
+                                    cell_slot_.bytes + acc_intra_.bytes + acc_w_.bytes + emit_maps_.bytes + emit_state_.bytes + csr_count_.bytes +
                                     csr_start_.bytes + csr_pts_.bytes},
         {"brick tables", g_key_.bytes + g_mask_.bytes + g_base_.bytes},
         {"level tables", sub_nodes_.bytes + out_points_.bytes + stage_off_.bytes + post_ii_.bytes + node_dst_.bytes +
@@ -582,6 +582,7 @@ uint64_t device_bytes(const MemoryTerms& t) {
     b += t.n * 4;                                                      // leaf sub-step words
     b += t.out_cap * per_cand;                                         // subsampling scratch
     b += (uint64_t)t.sms * t.slots * 16;                               // per-block brick tables
+    if (t.weighted) b += (uint64_t)kSplitEmitNodes * (kBrickMapBytes + 16);   // handed-over brick maps
     b += t.node_cap * (sizeof(SubNode) + 4 + 8 + 4 + 8 + 8 + 8 + 4);   // level tables, placement lists
     b += 3 * (t.chunk_grid + 2) * 8 + t.chunk_grid * 4 + 64 * 256;    // keys, spread, small buffers
     return b;
@@ -1117,6 +1118,8 @@ void Builder::subsample() {
             csr_count_.ensure(scratch_cap * 4);
             csr_start_.ensure(scratch_cap * 4);
             csr_pts_.ensure(scratch_cap * 20);
+            emit_maps_.ensure((size_t)kSplitEmitNodes * kBrickMapBytes);
+            emit_state_.ensure((size_t)kSplitEmitNodes * 16);
         }
         stage_lut_.ensure(stage_cap * 4);
         stage_rec_.ensure(stage_cap * 18 + 64);
@@ -1217,7 +1220,14 @@ void Builder::subsample() {
                 a.out_points = out_points_.as<uint32_t>() + first;
                 ClusterCaps caps;
                 caps.node_blocks = node_blocks[l];
+                // a distance-weighted level of few nodes hands each node's
+                // emit to k_emit_weighted, over all SMs
+                const bool split = weighted && cnt <= kSplitEmitNodes;
+                a.emit_maps = split ? emit_maps_.as<uint8_t>() : nullptr;
+                a.emit_state = split ? emit_state_.as<uint32_t>() : nullptr;
+                if (split) check_cuda(cudaMemsetAsync(emit_state_.p, 0, (size_t)cnt * 16, stream_), "memset");
                 launches_ += launch_subsample_level(a, num_sms_, balance[l], stream_, caps);
+                if (split) launches_ += launch_emit_weighted(a, num_sms_, stream_);
                 char mark[32];
                 std::snprintf(mark, sizeof mark, "sub_l%u", l);
                 stage_mark(mark);

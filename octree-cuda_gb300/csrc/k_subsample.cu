@@ -43,7 +43,7 @@ namespace {
 #define OC_SUB_THREADS 1024
 #endif
 constexpr int kSubThreads = OC_SUB_THREADS;
-constexpr uint32_t kBrickSlots = 8192;    // shared-memory brick table capacity
+constexpr uint32_t kBrickSlots = kSharedBrickSlots;   // shared-memory brick table capacity
 constexpr uint32_t kBrickShift = 32 - 13;
 
 struct BrickMap {
@@ -318,6 +318,100 @@ struct WeightedSum {
     }
 };
 
+// The node's children (their records' start, count and kind) and the
+// running candidate count before each child.
+__device__ __forceinline__ void load_node_shared(NodeShared& ns, const SubNode& nd) {
+    ns.nchild = nd.nchild;
+    ns.kind = nd.child_kind;
+    uint32_t p = 0;
+    for (uint32_t c = 0; c < nd.nchild; ++c) {
+        ns.start[c] = nd.child_start[c];
+        ns.count[c] = nd.child_count[c];
+        ns.prefix[c] = p;
+        p += nd.child_count[c];
+    }
+    ns.prefix[nd.nchild] = p;
+}
+
+// Distance-weighted emit of one node's cells: warps take runs of 16 cells
+// from *next until none is left.  Two lanes per cell, each walking every
+// other point of the neighbours' lists; their integer sums are combined by a
+// shuffle (any order gives the same sums), so a warp waits for the heaviest
+// of 16 cells instead of 32: 25.8M-point build 21.6 -> 20.8 ms (4 lanes per
+// cell: 26.7 ms, 8: 37.9 ms).  Every lane of the calling warps calls it.
+template <bool kRandom>
+__device__ __forceinline__ void emit_weighted(const SubLevelArgs& a, const BrickMap& bm, const NodeShared& ns,
+                                              uint64_t off, uint64_t oo, uint32_t cells, uint32_t* next) {
+    constexpr uint32_t kWG = 2u;
+    const uint32_t lane = threadIdx.x & 31, sub = lane % kWG;
+    for (;;) {
+        uint32_t r0 = 0;
+        if (lane == 0) r0 = atomicAdd(next, 32u / kWG);
+        r0 = __shfl_sync(0xffffffffu, r0, 0);
+        if (r0 >= cells) break;
+        const uint32_t r = r0 + lane / kWG;
+        uint32_t nw[5] = {0, 0, 0, 0, 0};
+        uint16_t cr = 0, cg = 0, cb = 0;
+        uint64_t sr = 0, sg = 0, sb = 0, sw = 0;
+        uint32_t idx = 0, csel = 0;
+        uint64_t spos = 0;
+        if (r < cells) {
+            const uint32_t ks = a.cell_slot[off + r];
+            const uint32_t slot = ks >> 6, bit = ks & 63;
+            const uint32_t brick = bm.key[slot] - 1;
+            const int bx = (int)(brick & 0xFF), by = (int)((brick >> 8) & 0xFF), bz = (int)(brick >> 16);
+            const int lx = (int)(bit & 3), ly = (int)((bit >> 2) & 3), lz = (int)((bit >> 4) & 3);
+            const uint64_t best = a.acc_best[off + r];
+            idx = kRandom ? (uint32_t)best : (uint32_t)(best >> 32);
+            const uint32_t jsel = kRandom ? a.acc_sel[off + r] : (uint32_t)best;
+#pragma unroll
+            for (uint32_t c = 1; c < 8; ++c) csel += (c < ns.nchild && ns.prefix[c] <= jsel) ? 1u : 0u;
+            spos = ns.start[csel] + (jsel - ns.prefix[csel]);
+            const uintptr_t sa =
+                reinterpret_cast<uintptr_t>((((ns.kind >> csel) & 1u) ? a.stage_rec : a.leaf_rec) + spos * 18);
+            const uint32_t* sq = reinterpret_cast<const uint32_t*>(sa & ~(uintptr_t)3);
+            const uint32_t sh = (uint32_t)(sa & 2) * 8;
+            const uint32_t q0 = sq[0], q1 = sq[1], q2 = sq[2], q3 = sq[3], q4 = sq[4];
+            nw[0] = __funnelshift_r(q0, q1, sh);
+            nw[1] = __funnelshift_r(q1, q2, sh);
+            nw[2] = __funnelshift_r(q2, q3, sh);
+            const uint32_t w3 = __funnelshift_r(q3, q4, sh);
+            cr = (uint16_t)w3;
+            cg = (uint16_t)(w3 >> 16);
+            cb = (uint16_t)(q4 >> sh);
+            WeightedSum f{a.csr_start + off, a.csr_count + off, a.csr_pts + off * 20,
+                          bx * 4 + lx, by * 4 + ly, bz * 4 + lz, 0, 0, 0, 0, sub, kWG};
+            visit_neighbours(bm, slot, bx, by, bz, lx, ly, lz, f);
+            sr = f.sr;
+            sg = f.sg;
+            sb = f.sb;
+            sw = f.sw;
+        }
+#pragma unroll
+        for (uint32_t o = kWG / 2; o >= 1; o >>= 1) {
+            sr += __shfl_xor_sync(0xffffffffu, sr, o);
+            sg += __shfl_xor_sync(0xffffffffu, sg, o);
+            sb += __shfl_xor_sync(0xffffffffu, sb, o);
+            sw += __shfl_xor_sync(0xffffffffu, sw, o);
+        }
+        if (r < cells && sub == 0) {
+            if (sw) {
+                cr = (uint16_t)(sr / sw);
+                cg = (uint16_t)(sg / sw);
+                cb = (uint16_t)(sb / sw);
+            }
+            a.out_lut[oo + r] = idx;
+            if (a.out_frac) {
+                const uint32_t* sf = ((ns.kind >> csel) & 1u) ? a.stage_frac : a.leaf_frac;
+                a.out_frac[oo + r] = sf ? sf[spos] : 0u;
+            }
+            nw[3] = (uint32_t)cr | ((uint32_t)cg << 16);
+            nw[4] = cb;
+            store_record_words(a.out_rec, oo + r, nw);
+        }
+    }
+}
+
 // kColor: 0 raw colour, 1 intra-cell, 2 inter-cell, 3 distance-weighted inter-cell.
 // kCluster: a thread-block cluster shares each node (levels with fewer nodes
 // than SMs).  The brick map, its counters and the node's cell count live in
@@ -412,18 +506,7 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a0, W
             gl_map.bs = sm_map.bs;
         }
         const SubNode& nd = kWave ? *wn.node[ni] : a.nodes[ni];
-        if (threadIdx.x == 0) {
-            ns.nchild = nd.nchild;
-            ns.kind = nd.child_kind;
-            uint32_t p = 0;
-            for (uint32_t c = 0; c < nd.nchild; ++c) {
-                ns.start[c] = nd.child_start[c];
-                ns.count[c] = nd.child_count[c];
-                ns.prefix[c] = p;
-                p += nd.child_count[c];
-            }
-            ns.prefix[nd.nchild] = p;
-        }
+        if (threadIdx.x == 0) load_node_shared(ns, nd);
         const AxisGrid ax0 = nd.ax[0], ax1 = nd.ax[1], ax2 = nd.ax[2];
         const QAxis qa0 = nd.qa[0], qa1 = nd.qa[1], qa2 = nd.qa[2];
         const uint64_t off = nd.cand_off;
@@ -431,6 +514,13 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a0, W
         const uint32_t level = nd.level;
         const uint64_t morton = nd.morton;
         BrickMap bm = sm_map;
+        if (weighted && a.emit_state) {
+            // a level that hands its emits over: each node its own global
+            // table, which stays intact for k_emit_weighted
+            gl_map.mask = a0.global_mask + (uint64_t)li * a0.global_cap;
+            gl_map.key = a0.global_key + (uint64_t)li * a0.global_cap;
+            gl_map.base = a0.global_base + (uint64_t)li * a0.global_cap;
+        }
 
         // ---- pass A: cells and occupancy.  A node whose bricks exceed 70% of
         // the shared table is redone with the block's global-memory table.
@@ -767,78 +857,28 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a0, W
         // that warps with light cells take more runs, and writes their
         // records with coalesced stores)
         if constexpr (weighted) {
-            // Distance weighting: two lanes per cell, each walking every other
-            // point of the neighbours' lists; their integer sums are combined
-            // by a shuffle (any order gives the same sums).  A warp then waits
-            // for the heaviest of 16 cells instead of 32: 25.8M-point build
-            // 21.6 -> 20.8 ms (4 lanes per cell: 26.7 ms, 8: 37.9 ms).
-            constexpr uint32_t kWG = 2u;
-            const uint32_t lane = threadIdx.x & 31, sub = lane % kWG;
-            for (;;) {
-                uint32_t r0 = 0;
-                if (lane == 0) r0 = atomicAdd(p_emit_next, 32u / kWG);
-                r0 = __shfl_sync(0xffffffffu, r0, 0);
-                if (r0 >= cells) break;
-                const uint32_t r = r0 + lane / kWG;
-                uint32_t nw[5] = {0, 0, 0, 0, 0};
-                uint16_t cr = 0, cg = 0, cb = 0;
-                uint64_t sr = 0, sg = 0, sb = 0, sw = 0;
-                uint32_t idx = 0, csel = 0;
-                uint64_t spos = 0;
-                if (r < cells) {
-                    const uint32_t ks = a.cell_slot[off + r];
-                    const uint32_t slot = ks >> 6, bit = ks & 63;
-                    const uint32_t brick = bm.key[slot] - 1;
-                    const int bx = (int)(brick & 0xFF), by = (int)((brick >> 8) & 0xFF), bz = (int)(brick >> 16);
-                    const int lx = (int)(bit & 3), ly = (int)((bit >> 2) & 3), lz = (int)((bit >> 4) & 3);
-                    const uint64_t best = a.acc_best[off + r];
-                    idx = random ? (uint32_t)best : (uint32_t)(best >> 32);
-                    const uint32_t jsel = random ? a.acc_sel[off + r] : (uint32_t)best;
-#pragma unroll
-                    for (uint32_t c = 1; c < 8; ++c) csel += (c < ns.nchild && ns.prefix[c] <= jsel) ? 1u : 0u;
-                    spos = ns.start[csel] + (jsel - ns.prefix[csel]);
-                    const uintptr_t sa =
-                        reinterpret_cast<uintptr_t>((((ns.kind >> csel) & 1u) ? a.stage_rec : a.leaf_rec) + spos * 18);
-                    const uint32_t* sq = reinterpret_cast<const uint32_t*>(sa & ~(uintptr_t)3);
-                    const uint32_t sh = (uint32_t)(sa & 2) * 8;
-                    const uint32_t q0 = sq[0], q1 = sq[1], q2 = sq[2], q3 = sq[3], q4 = sq[4];
-                    nw[0] = __funnelshift_r(q0, q1, sh);
-                    nw[1] = __funnelshift_r(q1, q2, sh);
-                    nw[2] = __funnelshift_r(q2, q3, sh);
-                    const uint32_t w3 = __funnelshift_r(q3, q4, sh);
-                    cr = (uint16_t)w3;
-                    cg = (uint16_t)(w3 >> 16);
-                    cb = (uint16_t)(q4 >> sh);
-                    WeightedSum f{a.csr_start + off, a.csr_count + off, a.csr_pts + off * 20,
-                                  bx * 4 + lx, by * 4 + ly, bz * 4 + lz, 0, 0, 0, 0, sub, kWG};
-                    visit_neighbours(bm, slot, bx, by, bz, lx, ly, lz, f);
-                    sr = f.sr;
-                    sg = f.sg;
-                    sb = f.sb;
-                    sw = f.sw;
-                }
-#pragma unroll
-                for (uint32_t o = kWG / 2; o >= 1; o >>= 1) {
-                    sr += __shfl_xor_sync(0xffffffffu, sr, o);
-                    sg += __shfl_xor_sync(0xffffffffu, sg, o);
-                    sb += __shfl_xor_sync(0xffffffffu, sb, o);
-                    sw += __shfl_xor_sync(0xffffffffu, sw, o);
-                }
-                if (r < cells && sub == 0) {
-                    if (sw) {
-                        cr = (uint16_t)(sr / sw);
-                        cg = (uint16_t)(sg / sw);
-                        cb = (uint16_t)(sb / sw);
+            if (a.emit_state) {
+                // a level of few nodes: k_emit_weighted spreads the node's
+                // cells over all SMs.  A shared-table node's brick map goes to
+                // global memory; a global-table node keeps its own table.
+                const bool shared_table = bm.key != gl_map.key;
+                if (shared_table) {
+                    uint8_t* dst = a.emit_maps + (uint64_t)li * kBrickMapBytes;
+                    uint64_t* dmask = reinterpret_cast<uint64_t*>(dst);
+                    uint32_t* dkey = reinterpret_cast<uint32_t*>(dst + (uint64_t)kBrickSlots * 8);
+                    uint32_t* dbase = dkey + kBrickSlots;
+                    for (uint32_t i = tid0; i < kBrickSlots; i += tstride) {
+                        dmask[i] = bm.mask[i];
+                        dkey[i] = bm.key[i];
+                        dbase[i] = bm.base[i];
                     }
-                    a.out_lut[oo + r] = idx;
-                    if (a.out_frac) {
-                        const uint32_t* sf = ((ns.kind >> csel) & 1u) ? a.stage_frac : a.leaf_frac;
-                        a.out_frac[oo + r] = sf ? sf[spos] : 0u;
-                    }
-                    nw[3] = (uint32_t)cr | ((uint32_t)cg << 16);
-                    nw[4] = cb;
-                    store_record_words(a.out_rec, oo + r, nw);
                 }
+                if (crank == 0 && threadIdx.x == 0) {
+                    a.emit_state[4 * li + 0] = cells;
+                    a.emit_state[4 * li + 2] = shared_table ? 1u : 2u;
+                }
+            } else {
+                emit_weighted<kRandom>(a, bm, ns, off, oo, cells, p_emit_next);
             }
         } else {
             for (;;) {
@@ -895,6 +935,62 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a0, W
         }
         if (crank == 0 && threadIdx.x == 0) a.out_points[li] = cells;
         sync_all();
+    }
+}
+
+// The emit of the distance-weighted nodes a level of few nodes handed over
+// (emit_state[4v + 2] set): every block takes runs of such a node's cells
+// with the node's brick map copied into its shared memory, so that the
+// node's cells spread over all SMs instead of its cluster's.
+template <bool kRandom>
+__global__ void __launch_bounds__(kSubThreads, 1) k_emit_weighted(SubLevelArgs a) {
+    extern __shared__ uint64_t dyn[];
+    __shared__ NodeShared ns;
+    __shared__ uint32_t s_take;
+    BrickMap bm;
+    bm.mask = dyn;
+    bm.key = reinterpret_cast<uint32_t*>(dyn + kBrickSlots);
+    bm.base = bm.key + kBrickSlots;
+    bm.cap = kBrickSlots;
+    bm.shift = kBrickShift;
+    bm.grid = a.grid;
+    bm.bs = (a.grid + 3) >> 2;
+    for (uint32_t v = 0; v < a.n_nodes; ++v) {
+        uint32_t* st = a.emit_state + 4 * v;
+        if (threadIdx.x == 0) {
+            const uint32_t cells = st[0];
+            s_take = st[2] != 0 && *(volatile uint32_t*)&st[1] < cells;
+            if (s_take) {
+                load_node_shared(ns, a.nodes[v]);
+                ns.cells = cells;
+            }
+        }
+        __syncthreads();
+        const bool take = s_take != 0;
+        __syncthreads();   // s_take is rewritten for the next node
+        if (!take) continue;
+        BrickMap m = bm;
+        if (st[2] == 1) {   // the node's shared-table map, into this block's shared memory
+            const uint8_t* src = a.emit_maps + (uint64_t)v * kBrickMapBytes;
+            const uint64_t* smask = reinterpret_cast<const uint64_t*>(src);
+            const uint32_t* skey = reinterpret_cast<const uint32_t*>(src + (uint64_t)kBrickSlots * 8);
+            const uint32_t* sbase = skey + kBrickSlots;
+            for (uint32_t i = threadIdx.x; i < kBrickSlots; i += blockDim.x) {
+                bm.mask[i] = smask[i];
+                bm.key[i] = skey[i];
+                bm.base[i] = sbase[i];
+            }
+        } else {   // the node's own global table
+            m.mask = a.global_mask + (uint64_t)v * a.global_cap;
+            m.key = a.global_key + (uint64_t)v * a.global_cap;
+            m.base = a.global_base + (uint64_t)v * a.global_cap;
+            m.cap = a.global_cap;
+            m.shift = a.global_shift;
+        }
+        __syncthreads();
+        const SubNode& nd = a.nodes[v];
+        emit_weighted<kRandom>(a, m, ns, nd.cand_off, nd.out_off, ns.cells, st + 1);
+        __syncthreads();   // the map and the node's metadata are rewritten for the next node
     }
 }
 
@@ -1148,6 +1244,20 @@ int launch_subsample_wave(const SubLevelArgs& wave, const WaveNodes& wn, int num
     const size_t smem = subsample_smem_bytes();
     if (wave.float_input) launch_mode<true, true>(wave, wn, num_sms, balance_blocks, smem, stream, caps);
     else launch_mode<false, true>(wave, wn, num_sms, balance_blocks, smem, stream, caps);
+    return 1;
+}
+
+int launch_emit_weighted(const SubLevelArgs& a, int num_sms, cudaStream_t stream) {
+    if (!a.n_nodes || !a.emit_state) return 0;
+    const size_t smem = (size_t)kBrickMapBytes;
+    const int grid = std::max(num_sms, 1);
+    if (a.mode & kModeRandom) {
+        allow_dynamic_smem(reinterpret_cast<const void*>(k_emit_weighted<true>), smem);
+        k_emit_weighted<true><<<grid, kSubThreads, smem, stream>>>(a);
+    } else {
+        allow_dynamic_smem(reinterpret_cast<const void*>(k_emit_weighted<false>), smem);
+        k_emit_weighted<false><<<grid, kSubThreads, smem, stream>>>(a);
+    }
     return 1;
 }
 

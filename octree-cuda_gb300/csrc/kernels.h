@@ -107,7 +107,12 @@ struct SubLevelArgs {
     uint32_t* acc_sel;          // per cell: winning candidate (explicit random)
     uint32_t* cell_slot;        // per cell: brick slot holding it
     uint64_t* acc_intra;        // per cell: packed colour sum
-    uint64_t* acc_inter;        // per cell: packed colour sum over the 3x3x3 neighbourhood
+    // Distance weighting on a level of few nodes: a node on the shared brick
+    // table copies its brick map to emit_maps and leaves its emit to
+    // k_emit_weighted, which spreads the node's cells over all SMs.  Null:
+    // every node emits in its own block or cluster.
+    uint8_t* emit_maps;         // per node of the level: kBrickMapBytes
+    uint32_t* emit_state;       // per node of the level: {cells, next run, handed over, 0}
     uint64_t* acc_w;            // per cell: 4 x fixed-point weighted sums (weighted only)
     uint32_t* csr_count;        // per cell: candidates in the cell (weighted only)
     uint32_t* csr_start;        // per cell
@@ -199,6 +204,13 @@ struct ClusterCaps {
     uint32_t node_blocks = 16;
 };
 constexpr uint64_t kCandidatesPerClusterBlock = 8192;
+// slots of the shared-memory brick table of a subsample block, and the bytes
+// of one table (64-bit mask, 32-bit key and rank base per slot)
+constexpr uint32_t kSharedBrickSlots = 8192;
+constexpr uint64_t kBrickMapBytes = (uint64_t)kSharedBrickSlots * 16;
+// distance-weighted levels of at most this many nodes spread each node's
+// emit over all SMs (k_emit_weighted)
+constexpr uint32_t kSplitEmitNodes = 16;
 // node_blocks for a level whose largest node has `max_bound` candidates
 inline uint32_t node_blocks_for(uint64_t max_bound) {
     uint32_t b = 1;
@@ -220,6 +232,9 @@ int launch_subsample_level(const SubLevelArgs& a, int num_sms, uint32_t balance_
 // capacity error set is skipped.
 int launch_subsample_wave(const SubLevelArgs& wave, const WaveNodes& wn, int num_sms, uint32_t balance_blocks,
                           cudaStream_t stream, const ClusterCaps& caps = ClusterCaps{});
+// The emit of the nodes a launch_subsample_level with emit_state handed
+// over, on num_sms blocks; launched right after it on the same stream.
+int launch_emit_weighted(const SubLevelArgs& a, int num_sms, cudaStream_t stream);
 
 // Raises a kernel's dynamic shared memory limit on the current device to at
 // least `bytes` and never lowers it, so that builders launching the same
