@@ -505,7 +505,7 @@ std::vector<std::pair<std::string, uint64_t>> Builder::device_allocations() cons
         {"staged LUT", stage_lut_.bytes},
         {"sub-step words", leaf_frac_.bytes + stage_frac_.bytes},
         {"subsampling scratch", key_cache_.bytes + unit_cache_.bytes + acc_best_.bytes + acc_sel_.bytes +
-                                    cell_slot_.bytes + acc_intra_.bytes + acc_w_.bytes + emit_maps_.bytes + emit_state_.bytes + csr_count_.bytes +
+                                    cell_slot_.bytes + acc_intra_.bytes + emit_maps_.bytes + emit_state_.bytes + csr_count_.bytes +
                                     csr_start_.bytes + csr_pts_.bytes},
         {"brick tables", g_key_.bytes + g_mask_.bytes + g_base_.bytes},
         {"level tables", sub_nodes_.bytes + out_points_.bytes + stage_off_.bytes + post_ii_.bytes + node_dst_.bytes +

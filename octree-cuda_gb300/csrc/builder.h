@@ -273,7 +273,7 @@ private:
     DevBuf lut_, rec_;                  // final outputs (N + P_out records)
     DevBuf stage_lut_, stage_rec_;      // staged internal outputs
     DevBuf sub_nodes_, out_points_, work_;
-    DevBuf key_cache_, unit_cache_, acc_best_, acc_sel_, cell_slot_, acc_intra_, acc_w_, emit_maps_, emit_state_, csr_count_, csr_start_, csr_pts_;
+    DevBuf key_cache_, unit_cache_, acc_best_, acc_sel_, cell_slot_, acc_intra_, emit_maps_, emit_state_, csr_count_, csr_start_, csr_pts_;
     DevBuf place_src_, place_dst_, place_cnt_;
     DevBuf g_key_, g_mask_, g_base_;   // per-block global brick tables
     DevBuf cell_keys_, spread_;         // chunking-grid boundary keys and Morton spread table

@@ -113,7 +113,6 @@ struct SubLevelArgs {
     // every node emits in its own block or cluster.
     uint8_t* emit_maps;         // per node of the level: kBrickMapBytes
     uint32_t* emit_state;       // per node of the level: {cells, next run, handed over, 0}
-    uint64_t* acc_w;            // per cell: 4 x fixed-point weighted sums (weighted only)
     uint32_t* csr_count;        // per cell: candidates in the cell (weighted only)
     uint32_t* csr_start;        // per cell
     uint8_t* csr_pts;           // per candidate: grouped by cell (weighted only), 20 bytes each
