@@ -939,9 +939,10 @@ __global__ void __launch_bounds__(kSubThreads, 1) k_subsample(SubLevelArgs a0, W
 }
 
 // The emit of the distance-weighted nodes a level of few nodes handed over
-// (emit_state[4v + 2] set): every block takes runs of such a node's cells
-// with the node's brick map copied into its shared memory, so that the
-// node's cells spread over all SMs instead of its cluster's.
+// (emit_state[4v + 2] set): every block takes runs of such a node's cells,
+// with the node's brick map copied into its shared memory (or read from the
+// node's own global table), so that the node's cells spread over all SMs
+// instead of its cluster's.
 template <bool kRandom>
 __global__ void __launch_bounds__(kSubThreads, 1) k_emit_weighted(SubLevelArgs a) {
     extern __shared__ uint64_t dyn[];

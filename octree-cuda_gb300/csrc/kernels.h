@@ -107,12 +107,15 @@ struct SubLevelArgs {
     uint32_t* acc_sel;          // per cell: winning candidate (explicit random)
     uint32_t* cell_slot;        // per cell: brick slot holding it
     uint64_t* acc_intra;        // per cell: packed colour sum
-    // Distance weighting on a level of few nodes: a node on the shared brick
-    // table copies its brick map to emit_maps and leaves its emit to
-    // k_emit_weighted, which spreads the node's cells over all SMs.  Null:
-    // every node emits in its own block or cluster.
+    // Distance weighting on a level of few nodes: each node leaves its emit to
+    // k_emit_weighted, which spreads the node's cells over all SMs.  A node on
+    // the shared brick table copies its map to emit_maps; a node on a global
+    // table uses the level's table number li (one per node), which stays
+    // intact.  Null: every node emits in its own block or cluster.
     uint8_t* emit_maps;         // per node of the level: kBrickMapBytes
-    uint32_t* emit_state;       // per node of the level: {cells, next run, handed over, 0}
+    // per node of the level: {cells, next run, 1 = map in emit_maps or
+    // 2 = its own global table (0: emitted in its cluster), 0}
+    uint32_t* emit_state;
     uint32_t* csr_count;        // per cell: candidates in the cell (weighted only)
     uint32_t* csr_start;        // per cell
     uint8_t* csr_pts;           // per candidate: grouped by cell (weighted only), 20 bytes each
