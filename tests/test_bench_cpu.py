@@ -1,6 +1,7 @@
-"""The reference arm of bench.py (the multithreaded CPU oracle on a bounded
-sample of the headline cloud) runs without a GPU and prints one JSON line
-with the keys of the measurement contract."""
+"""bench.py without a GPU: the reference arm (the multithreaded CPU oracle on
+a bounded sample of the headline cloud) prints one JSON line with the keys of
+the measurement contract, and the export timing of the GPU arm counts and
+removes what it wrote."""
 import json
 import os
 import subprocess
@@ -27,3 +28,26 @@ def test_reference_arm_prints_one_contract_line():
     e2e = line["e2e"]
     assert e2e["value"] == line["value"] and e2e["unit"] == line["unit"]
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+
+
+def test_export_timing_reports_bytes_and_removes_the_files(tmp_path, monkeypatch):
+    """bench.py's export field: one export into a scratch directory, its
+    bytes counted and the files removed; skipped when the scratch file
+    system cannot hold twice the records."""
+    import tempfile
+
+    sys.path.insert(0, ROOT)
+    import bench
+
+    monkeypatch.setattr(tempfile, "tempdir", str(tmp_path))
+
+    class FakeSession:
+        def export_potree(self, directory):
+            for name, size in (("hierarchy.bin", 44), ("octree.bin", 1800), ("metadata.json", 10)):
+                with open(os.path.join(directory, name), "wb") as f:
+                    f.write(b"\0" * size)
+
+    r = bench.export_timing(FakeSession(), 100)
+    assert r["bytes"] == 1854 and r["ms"] >= 0 and r["gbs"] >= 0
+    assert os.listdir(tmp_path) == []
+    assert "skipped" in bench.export_timing(FakeSession(), 10 ** 18)
