@@ -1125,37 +1125,14 @@ int cluster_slots(const void* kernel, size_t smem, uint32_t c) {
     return m;
 }
 
-// Cluster size for a distance-weighted level: the c (1 to cap) with the
-// smallest estimated level time
-//     max(1 / resident blocks(c), r / c) * g(c)
-// where resident blocks(c) = min(n_nodes, slots(c)) * c, r = the largest
-// node's share of the level's candidates (balance / num_sms) and g(c) the
-// per-block cost of cluster-wide work, fitted to measured levels: one-node
-// and 8-node levels of the 25.8M-point weighted build ran 1.29x and 1.74x
-// (root) and 1.62x and 2.15x (8 nodes) longer per block at clusters of 8 and
-// 16 than at 4, about c^0.4.  On a GPU that holds 9 clusters of 16 this
-// gives the largest node at least its share of the blocks, the rule used
-// before; on one that holds fewer, many-node levels take smaller clusters.
+// Cluster size for a distance-weighted level (weighted_cluster_choice), from
+// the clusters of 2, 4, 8 and 16 blocks of the kernel the device holds.
 uint32_t weighted_cluster_size(const void* cluster_kernel, size_t smem, uint32_t n_nodes, int num_sms,
                                uint32_t balance, uint32_t cap) {
-    static const double g[5] = {1.0, 1.32, 1.74, 2.30, 3.03};
-    const double r = (double)balance / (double)std::max(num_sms, 1);
-    uint32_t best = 1;
-    double best_t = std::max(1.0 / (double)std::min<uint32_t>(n_nodes, (uint32_t)num_sms), r);
-    int i = 1;
-    // never more blocks than the caller's SMs (the allocation-free entry
-    // point subsamples its node in one block)
-    for (uint32_t c = 2; c <= cap && c <= (uint32_t)std::max(num_sms, 1) && i < 5; c <<= 1, ++i) {
-        const int s = cluster_slots(cluster_kernel, smem, c);
-        if (s <= 0) break;
-        const double blocks = (double)std::min<uint32_t>(n_nodes, (uint32_t)s) * c;
-        const double t = std::max(1.0 / blocks, r / c) * g[i];
-        if (t < best_t) {
-            best_t = t;
-            best = c;
-        }
-    }
-    return best;
+    int slots[5] = {0, 0, 0, 0, 0};
+    for (uint32_t c = 2, i = 1; c <= cap && c <= (uint32_t)std::max(num_sms, 1) && i < 5; c <<= 1, ++i)
+        slots[i] = cluster_slots(cluster_kernel, smem, c);
+    return weighted_cluster_choice(slots, n_nodes, num_sms, balance, cap);
 }
 
 template <bool kF32, int kColor, bool kRandom, bool kWave>

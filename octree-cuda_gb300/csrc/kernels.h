@@ -5,6 +5,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 
@@ -222,6 +223,41 @@ inline uint32_t node_blocks_for(uint64_t max_bound) {
 
 size_t subsample_smem_bytes();
 uint32_t subsample_block_size();
+
+// Cluster size for a distance-weighted level: the c (1 to cap, at most
+// num_sms) with the smallest estimated level time
+//     max(1 / resident blocks(c), r / c) * g(c)
+// where resident blocks(c) = min(n_nodes, slots[log2 c]) * c, slots[i] the
+// clusters of 2^i blocks the device holds at once (a cluster must fit in one
+// GPC, so this differs between chips), r = the largest node's share of the
+// level's candidates (balance / num_sms) and g(c) the per-block cost of
+// cluster-wide work, fitted to measured levels: one-node and 8-node levels of
+// the 25.8M-point weighted build ran 1.29x and 1.74x (root) and 1.62x and
+// 2.15x (8 nodes) longer per block at clusters of 8 and 16 than at 4, about
+// c^0.4.  On a GPU that holds 7 clusters of 16 this gives the largest node at
+// least its share of the blocks; on one that holds fewer, levels of many
+// nodes take smaller clusters.  The allocation-free entry point passes
+// num_sms = 1 and gets one block.
+inline uint32_t weighted_cluster_choice(const int slots[5], uint32_t n_nodes, int num_sms, uint32_t balance,
+                                        uint32_t cap) {
+    static const double g[5] = {1.0, 1.32, 1.74, 2.30, 3.03};
+    const uint32_t sms = (uint32_t)(num_sms > 1 ? num_sms : 1);
+    const double r = (double)balance / (double)sms;
+    uint32_t best = 1;
+    double best_t = std::max(1.0 / (double)std::min(n_nodes, sms), r);
+    int i = 1;
+    for (uint32_t c = 2; c <= cap && c <= sms && i < 5; c <<= 1, ++i) {
+        const int s = slots[i];
+        if (s <= 0) break;
+        const double blocks = (double)std::min(n_nodes, (uint32_t)s) * c;
+        const double t = std::max(1.0 / blocks, r / c) * g[i];
+        if (t < best_t) {
+            best_t = t;
+            best = c;
+        }
+    }
+    return best;
+}
 // balance_blocks: the blocks the level's largest node needs for its share
 // of the work to equal one SM's share of the whole level (largest candidate
 // bound x SMs / sum of the bounds); distance-weighted levels size their
